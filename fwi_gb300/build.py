@@ -1,0 +1,83 @@
+"""Builds libfwi_gb300.so (sm_103a) in-tree: fwi_gb300/lib/libfwi_gb300.so.
+
+Translation units compile in parallel with one -gencode (compute_103a ->
+sm_103a); objects go to fwi_gb300/_build/.  No cmake, no torch extension
+machinery: plain nvcc, so the same recipe runs on x86 and aarch64 hosts.
+
+    python -m fwi_gb300.build [--force] [-j N]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIBDIR = os.path.join(PKG, "lib")
+LIB = os.path.join(LIBDIR, "libfwi_gb300.so")
+
+UNITS = ["compat.cu", "native.cu", "prop_f32.cu", "prop_f64.cu"]
+HEADERS = ["common.cuh", "tile.cuh", "prop.h", "prop.cuh"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force: bool = False, jobs: int = 4, verbose: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    inc = os.path.join(os.path.dirname(PKG), "include")
+    headers = [os.path.join(CSRC, h) for h in HEADERS] + [
+        os.path.join(inc, h) for h in os.listdir(inc) if h.endswith(".h")]
+    objs, todo = [], []
+    for u in UNITS:
+        src = os.path.join(CSRC, u)
+        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            todo.append([nvcc(), *ARCH, *NVCC_FLAGS, "-I", inc, "-c", src, "-o", obj])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{p.stdout}\n{p.stderr}")
+        return p
+
+    with ThreadPoolExecutor(max_workers=max(1, jobs)) as ex:
+        list(ex.map(run, todo))
+    if force or todo or _stale(LIB, objs):
+        run([nvcc(), *ARCH, "-shared", "--cudart", "static", "-o", LIB, *objs])
+    return LIB
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("-j", type=int, default=4)
+    ap.add_argument("-v", action="store_true")
+    a = ap.parse_args(argv)
+    print(build(force=a.force, jobs=a.j, verbose=a.v))
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,1084 @@
+// Native context of the FWI gradient library (include/fwi.h).
+//
+// One context = one device, one stream, one arena of device memory.  A
+// gradient call runs the shots in batches of up to max_shots:
+//   forward (2 launches / step, images kept per the storage mode)
+//   -> residual + FP64 misfit partials
+//   -> adjoint + imaging (2 launches / step)
+//   -> deterministic reduction of the per-shot gradients into the model grid.
+// The L-BFGS update of src/main.c:539-800 runs on the device with FP64 dot
+// products reduced by the last block to finish (no host round trip).
+#include "../../include/fwi.h"
+#include "common.cuh"
+#include "prop.h"
+
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+using fwi::Batch;
+using fwi::DevShot;
+
+int status_from_cuda(cudaError_t e)
+{
+    if (e == cudaSuccess) return FWI_OK;
+    if (e == cudaErrorMemoryAllocation) return FWI_ERR_NOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+        return FWI_ERR_NODEVICE;
+    return FWI_ERR_CUDA;
+}
+
+constexpr int kLayer = 15;  // near-surface rows never updated (include/parallelcalls.h:6)
+constexpr int kMaxHist = 16;
+constexpr int kRedBlocks = 304;  // reduction grid: 2 blocks per SM of a 152-SM GB300
+constexpr int kRedThreads = 256;
+
+long round_up(long v, long m) { return (v + m - 1) / m * m; }
+
+// ------------------------------------------------------------------ small kernels
+
+template <typename T>
+__global__ void k_scale_models(const T *vh, const T *vp, const T *vn, T *mh, T *mp, T *mn, T dt2, long n)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        mh[i] = dt2 * vh[i];
+        mp[i] = dt2 * vp[i];
+        mn[i] = dt2 * vn[i];
+    }
+}
+
+template <typename T>
+__global__ void k_pre_variables(const T *vel, const T *eps, const T *del, T *vh, T *vp, T *vn, int nx,
+                                int nz, int mpitch)
+{
+    long n = (long)nx * nz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        long iz = k / nx, ix = k - iz * nx, i = iz * mpitch + ix;
+        T v2 = vel[k] * vel[k];
+        vp[i] = v2;
+        vh[i] = v2 * (T(1) + T(2) * eps[k]);
+        vn[i] = v2 * (T(1) + T(2) * del[k]);
+    }
+}
+
+// CPML a, b by distance d = 1..cpml into the layer (src/parallelcalls.cu:25-26):
+// d0 Vmax (d dh / L)^2 and pi f (L - d dh) / L in FP64 from T inputs, b
+// rounded to T before a = d (b - 1) / (d + alpha) is formed, as the reference
+// does with T = float.
+template <typename T>
+__global__ void k_cpml_table(T *a, T *b, int cpml, T vmax, T dt, T dh, T f, T d0, T L)
+{
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d > cpml) return;
+    if (d == 0) { a[0] = T(0); b[0] = T(0); return; }
+    T frac = d * dh / L;
+    double dd = (double)(d0 * vmax) * ((double)frac * (double)frac);
+    double al = 3.141592653589793 * (double)f * (double)(L - d * dh) / (double)L;
+    T bT = (T)exp(-(dd + al) * (double)dt);
+    b[d] = bT;
+    a[d] = (T)(dd * (double)(bT - T(1)) / (dd + al));
+}
+
+// rec := mask (rec - obs); per-block partial sums of rec^2 (FP64).
+template <typename T>
+__global__ void k_residual(T *rec, const T *obs, const unsigned char *mask, const DevShot *shots,
+                           const long *mask_off, double *partial)
+{
+    const int s = blockIdx.y;
+    const DevShot sh = shots[s];
+    const int nrec = sh.rx1 - sh.rx0;
+    const long n = (long)sh.nt * nrec;
+    double acc = 0.0;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const long e = sh.rec_off + k;
+        T d = rec[e] - obs[e];
+        if (mask && !mask[mask_off[s] + (k % nrec)]) d = T(0);
+        rec[e] = d;
+        acc += (double)d * (double)d;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ double w[32];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += w[q];
+        partial[(long)s * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// misfit += 1/2 sum of partials, in a fixed order
+__global__ void k_misfit_finish(const double *partial, long n, double *misfit)
+{
+    __shared__ double w[32];
+    double acc = 0.0;
+    for (long k = threadIdx.x; k < n; k += blockDim.x) acc += partial[k];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += w[q];
+        *misfit += 0.5 * t;
+    }
+}
+
+// grad[iz][X] += sum over the batch's shots of their local gradients (fixed shot order).
+template <typename T>
+__global__ void k_accumulate_gradient(T *gh, T *gp, T *gn, const T *sh_h, const T *sh_p, const T *sh_n,
+                                      const DevShot *shots, int B, int nx, int nz, int mpitch, int pitch,
+                                      long slot)
+{
+    const long n = (long)nx * nz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const int iz = (int)(k / nx), X = (int)(k - (long)iz * nx);
+        T a = T(0), b = T(0), c = T(0);
+        for (int s = 0; s < B; s++) {
+            const int lx = X - shots[s].x0;
+            if (lx < 0 || lx >= shots[s].nx) continue;
+            const long i = (long)s * slot + (long)iz * pitch + lx;
+            a += sh_h[i];
+            b += sh_p[i];
+            c += sh_n[i];
+        }
+        const long o = (long)iz * mpitch + X;
+        gh[o] += a;
+        gp[o] += b;
+        gn[o] += c;
+    }
+}
+
+// ------------------------------------------------------------------ L-BFGS on the device
+
+// Three-parameter dot products with a last-block-done FP64 reduction.
+struct DotScratch {
+    double *partial;    // [kRedBlocks][4][3]
+    unsigned *counter;  // one per kernel sequence position
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Reduces up to 4 x 3 per-thread values into partial[block], then the last
+// block to arrive sums all partials in block order into out[4][3].
+__device__ void reduce_last_block(double (&v)[4][3], int nv, DotScratch ds, double *out)
+{
+    __shared__ double sm[8][12];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int a = 0; a < nv; a++)
+        for (int p = 0; p < 3; p++) {
+            double t = warp_sum(v[a][p]);
+            if (lane == 0) sm[warp][a * 3 + p] = t;
+        }
+    __syncthreads();
+    if (threadIdx.x < nv * 3) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w][threadIdx.x];
+        ds.partial[(long)blockIdx.x * 12 + threadIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(ds.counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < nv * 3) {
+        double t = 0.0;
+        for (int bI = 0; bI < (int)gridDim.x; bI++) t += ((volatile double *)ds.partial)[(long)bI * 12 + threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) *ds.counter = 0u;
+}
+
+template <typename T> struct Tri {
+    T *p[3];
+};
+template <typename T> struct CTri {
+    const T *p[3];
+};
+
+// s_k = m - m_back, y_k = g - g_back (3 parameters), and the dots y.s, y.y, s.g.
+template <typename T>
+__global__ void k_lb_pair(Tri<T> s, Tri<T> y, CTri<T> m, CTri<T> mb, CTri<T> g, CTri<T> gb, long n,
+                          DotScratch ds, double *out)
+{
+    double v[4][3] = {};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        for (int p = 0; p < 3; p++) {
+            T sv = m.p[p][i] - mb.p[p][i], yv = g.p[p][i] - gb.p[p][i];
+            s.p[p][i] = sv;
+            y.p[p][i] = yv;
+            v[0][p] += (double)yv * sv;
+            v[1][p] += (double)yv * yv;
+            v[2][p] += (double)sv * g.p[p][i];
+        }
+    reduce_last_block(v, 3, ds, out);
+}
+
+// v := w (copy) and the dots a.w for the first loop's first slot.
+template <typename T>
+__global__ void k_lb_copy_dot(Tri<T> dst, CTri<T> src, CTri<T> a, long n, DotScratch ds, double *out)
+{
+    double v[4][3] = {};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        for (int p = 0; p < 3; p++) {
+            T w = src.p[p][i];
+            dst.p[p][i] = w;
+            v[0][p] += (double)a.p[p][i] * w;
+        }
+    reduce_last_block(v, 1, ds, out);
+}
+
+// x := c0 * x + c1 * u (per-parameter scalars from device memory, FP64), then
+// the dots b.x for the next step (b may be null).
+template <typename T>
+__global__ void k_lb_axpy_dot(Tri<T> x, CTri<T> u, const double *c0, const double *c1, CTri<T> bnext,
+                              int has_next, long n, DotScratch ds, double *out)
+{
+    double v[4][3] = {};
+    double k0[3], k1[3];
+    for (int p = 0; p < 3; p++) { k0[p] = c0 ? c0[p] : 1.0; k1[p] = c1 ? c1[p] : 0.0; }
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        for (int p = 0; p < 3; p++) {
+            T xv = (T)(k0[p] * (double)x.p[p][i] + (u.p[p] ? k1[p] * (double)u.p[p][i] : 0.0));
+            x.p[p][i] = xv;
+            if (has_next) v[0][p] += (double)bnext.p[p][i] * xv;
+        }
+    if (has_next) reduce_last_block(v, 1, ds, out);
+}
+
+// Scalar bookkeeping of the two-loop recursion (one thread).
+struct LbScalars {
+    double rho[3][kMaxHist];
+    double alpha[3][kMaxHist];
+    double gamma[3];
+    double coefA[3], coefB[3];  // scratch coefficients for the next axpy
+    double dots[12];
+    double pair[12];            // y.s, y.y, s.g of the newest pair
+};
+
+// mode 0: newest pair formed: rho_k = 1/(y.s), first-loop alpha_k = rho_k (s_k.q) with q = g
+// mode 1: alpha_l = rho_l (s_l.q) from dots[0..2]
+// mode 2: gamma = (s.y)/(y.y); coefA = gamma
+// mode 3: beta = rho_l (y_l.r) from dots; coefB = alpha_l - beta
+__global__ void k_lb_scalar(LbScalars *S, int mode, int slot)
+{
+    if (threadIdx.x != 0) return;
+    for (int p = 0; p < 3; p++) {
+        if (mode == 0) {
+            S->rho[p][slot] = 1.0 / S->pair[p];
+            S->alpha[p][slot] = S->rho[p][slot] * S->pair[6 + p];
+            S->coefB[p] = -S->alpha[p][slot];
+        } else if (mode == 1) {
+            S->alpha[p][slot] = S->rho[p][slot] * S->dots[p];
+            S->coefB[p] = -S->alpha[p][slot];
+        } else if (mode == 2) {
+            S->gamma[p] = S->pair[p] / S->pair[3 + p];
+            S->coefA[p] = S->gamma[p];
+        } else {
+            double beta = S->rho[p][slot] * S->dots[p];
+            S->coefB[p] = S->alpha[p][slot] - beta;
+        }
+    }
+}
+
+// First-iteration scale 1/|g| (src/main.c:551-561).
+__global__ void k_lb_inv_norm(LbScalars *S)
+{
+    if (threadIdx.x != 0) return;
+    for (int p = 0; p < 3; p++) S->coefA[p] = 1.0 / sqrt(S->dots[p]);
+}
+
+// v -= a_p * g * coefA_p below the layer, v_hor >= v_nmo (src/parallelcalls.cu:273-286).
+template <typename T>
+__global__ void k_first_update(T *vh, T *vp, T *vn, const T *gh, const T *gp, const T *gn, const LbScalars *S,
+                               float a_hor, float a_po, float a_nmo, int nx, int nz, int mpitch)
+{
+    long n = (long)nx * (nz - kLayer - 1);
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        long iz = kLayer + 1 + k / nx, ix = k % nx, i = iz * mpitch + ix;
+        vp[i] = vp[i] - (T)(a_po * (gp[i] * S->coefA[1]));
+        T vnn = vn[i] - (T)(a_nmo * (gn[i] * S->coefA[2]));
+        T vhn = vh[i] - (T)(a_hor * (gh[i] * S->coefA[0]));
+        vn[i] = vnn;
+        vh[i] = vhn < vnn ? vnn : vhn;
+    }
+}
+
+// Trial model (src/parallelcalls.cu:343-404) for all three parameters.
+template <typename T>
+__global__ void k_lb_update(T *vh, T *vp, T *vn, const T *bh, const T *bp, const T *bn, const T *rh,
+                            const T *rp, const T *rn, float av, float ad, float ae, int fmin, int fmax,
+                            int nx, int nz, int mpitch)
+{
+    long n = (long)nx * (nz - kLayer - 1);
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        long iz = kLayer + 1 + k / nx, ix = k % nx, i = iz * mpitch + ix;
+        T p = bp[i] - (T)av * rp[i];
+        if (fmax == 1 && p > T(3.5e6)) p = T(3.5e6);
+        if (fmin == 1 && p < T(1.8e6)) p = T(1.8e6);
+        vp[i] = p;
+        T q = bn[i] - (T)ad * rn[i];
+        if (fmax == 1 && q > T(4e6)) q = T(4e6);
+        if (fmin == 1 && q < T(1.8e6)) q = T(1.8e6);
+        vn[i] = q;
+        T h = bh[i] - (T)ae * rh[i];
+        if (fmax == 1 && h > T(4.5e6)) h = T(4.5e6);
+        if (fmin == 1 && h < T(1.8e6)) h = T(1.8e6);
+        vh[i] = h < q ? q : h;
+    }
+}
+
+// dJ/dVp, dJ/deps, dJ/ddelta from the squared-velocity gradients.
+template <typename T>
+__global__ void k_grad_vti(const T *vh, const T *vp, const T *vn, const T *gh, const T *gp, const T *gn, T *ovp,
+                           T *oeps, T *odel, int nx, int nz, int mpitch)
+{
+    long n = (long)nx * nz;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        long iz = k / nx, ix = k - iz * nx, i = iz * mpitch + ix;
+        T v2 = vp[i];
+        T vel = sqrt(v2);
+        T ope = vh[i] / v2, opd = vn[i] / v2;  // 1 + 2 eps, 1 + 2 delta
+        ovp[i] = T(2) * vel * (gp[i] + ope * gh[i] + opd * gn[i]);
+        oeps[i] = T(2) * v2 * gh[i];
+        odel[i] = T(2) * v2 * gn[i];
+    }
+}
+
+inline unsigned elt_grid(long n)
+{
+    long b = (n + 255) / 256;
+    return (unsigned)std::max(1L, std::min(b, 152L * 8));
+}
+
+// ------------------------------------------------------------------ the context
+
+struct CtxBase {
+    fwi_config cfg{};
+    int last_cuda = 0;
+    float timing[4] = {0, 0, 0, 0};
+    long launches = 0;
+    virtual ~CtxBase() {}
+    virtual int init() = 0;
+    virtual int set_model(const void *, const void *, const void *) = 0;
+    virtual int set_model_vti(const void *, const void *, const void *) = 0;
+    virtual int get_model(void *, void *, void *) = 0;
+    virtual int set_wavelet(const void *, int) = 0;
+    virtual int set_ricker(float, int) = 0;
+    virtual int run(const fwi_shot *, int, const void *, const unsigned char *, void *, void *, void *,
+                    double *, void *traces, bool grad) = 0;
+    virtual int first_step(float, float, float) = 0;
+    virtual int lbfgs_direction(int, double *) = 0;
+    virtual int lbfgs_update(float, float, float, int, int) = 0;
+    virtual int restore_model() = 0;
+    virtual int gradient_vti(void *, void *, void *) = 0;
+    virtual int set_gradient(const void *, const void *, const void *) = 0;
+    int fail(cudaError_t e)
+    {
+        last_cuda = (int)e;
+        cudaGetLastError();
+        return status_from_cuda(e);
+    }
+};
+
+#define TRY(expr)                                        \
+    do {                                                 \
+        cudaError_t e_ = (expr);                         \
+        if (e_ != cudaSuccess) return fail(e_);          \
+    } while (0)
+#define TRY_LAUNCH() TRY(cudaGetLastError())
+
+template <typename T> struct Ctx : CtxBase {
+    int nx = 0, nz = 0, mpitch = 0, pitch = 0, B = 0, nt_max = 0, nrec_max = 0, n_img = 0;
+    long slot = 0, mslot = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[4] = {};
+    std::vector<void *> allocs;
+    // model and setup
+    T *vh = nullptr, *vp = nullptr, *vn = nullptr, *mh = nullptr, *mp = nullptr, *mn = nullptr;
+    T *cpa = nullptr, *cpb = nullptr, *wavelet = nullptr;
+    bool have_model = false, have_wavelet = false, models_dirty = true;
+    int wavelet_nt = 0;
+    // batch
+    T *lvl[4] = {}, *cp[8] = {}, *gs[3] = {};
+    void *store = nullptr;
+    float *scale = nullptr, *amax = nullptr;
+    T *rec = nullptr, *obs = nullptr;
+    unsigned char *mask = nullptr;
+    long *mask_off = nullptr;
+    DevShot *shots = nullptr;
+    unsigned *status = nullptr;
+    double *partial = nullptr, *misfit = nullptr;
+    // gradient and L-BFGS
+    T *grad[3] = {};
+    bool have_grad = false;
+    T *mb[3] = {}, *gb[3] = {}, *q[3] = {}, *r[3] = {};
+    T *hs[kMaxHist][3] = {}, *hy[kMaxHist][3] = {};
+    int hist_m = 0, hist_count = 0, hist_next = 0;
+    bool have_back = false;
+    LbScalars *lbs = nullptr;
+    DotScratch ds{};
+    T *vti_out[3] = {};
+
+    ~Ctx() override
+    {
+        if (st) cudaStreamSynchronize(st);
+        for (void *p : allocs) cudaFree(p);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    template <typename U> cudaError_t alloc(U **p, size_t count)
+    {
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(U));
+        if (e == cudaSuccess) allocs.push_back(q);
+        *p = (U *)q;
+        return e;
+    }
+
+    int store_type() const
+    {
+        if (cfg.store_prec == FWI_SPREC_FP16) return fwi::kStoreHalf;
+        if (cfg.store_prec == FWI_SPREC_BF16) return fwi::kStoreBf16;
+        return fwi::kStoreNative;
+    }
+    size_t store_elem() const { return store_type() == fwi::kStoreNative ? sizeof(T) : 2; }
+
+    int init() override
+    {
+        nx = cfg.nx;
+        nz = cfg.nz;
+        mpitch = (int)round_up(nx, 32);
+        const int win = cfg.max_window > 0 ? cfg.max_window : nx;
+        pitch = (int)round_up(win, 32);
+        B = cfg.max_shots;
+        nt_max = cfg.nt_max;
+        nrec_max = cfg.max_receivers > 0 ? cfg.max_receivers : win;
+        slot = (long)nz * pitch;
+        mslot = (long)nz * mpitch;
+        n_img = nt_max;
+        TRY(cudaSetDevice(cfg.device));
+        TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        for (auto &e : ev) TRY(cudaEventCreate(&e));
+        for (T **p : {&vh, &vp, &vn, &mh, &mp, &mn}) TRY(alloc(p, mslot));
+        TRY(alloc(&cpa, cfg.cpml + 1));
+        TRY(alloc(&cpb, cfg.cpml + 1));
+        TRY(alloc(&wavelet, nt_max));
+        for (auto &p : lvl) TRY(alloc(&p, (size_t)B * slot));
+        for (auto &p : cp) TRY(alloc(&p, (size_t)B * slot));
+        for (auto &p : gs) TRY(alloc(&p, (size_t)B * slot));
+        {
+            void *q0 = nullptr;
+            TRY(cudaMalloc(&q0, (size_t)B * n_img * 2 * slot * store_elem()));
+            allocs.push_back(q0);
+            store = q0;
+        }
+        TRY(alloc(&scale, (size_t)B * nt_max));
+        TRY(alloc(&amax, (size_t)B * (nt_max + 1)));
+        TRY(alloc(&rec, (size_t)B * nt_max * nrec_max));
+        TRY(alloc(&obs, (size_t)B * nt_max * nrec_max));
+        TRY(alloc(&mask, (size_t)B * nrec_max));
+        TRY(alloc(&mask_off, B));
+        TRY(alloc(&shots, B));
+        TRY(alloc(&status, 1));
+        TRY(alloc(&partial, (size_t)B * kRedBlocks));
+        TRY(alloc(&misfit, 1));
+        for (auto &p : grad) TRY(alloc(&p, mslot));
+        for (T **p : {&mb[0], &mb[1], &mb[2], &gb[0], &gb[1], &gb[2], &q[0], &q[1], &q[2], &r[0], &r[1], &r[2]})
+            TRY(alloc(p, mslot));
+        TRY(alloc(&lbs, 1));
+        TRY(alloc(&ds.partial, (size_t)kRedBlocks * 12));
+        TRY(alloc(&ds.counter, 1));
+        TRY(cudaMemsetAsync(ds.counter, 0, sizeof(unsigned), st));
+        TRY(cudaMemsetAsync(lbs, 0, sizeof(LbScalars), st));
+        for (T *p : {vh, vp, vn, mh, mp, mn}) TRY(cudaMemsetAsync(p, 0, mslot * sizeof(T), st));
+        // CPML table by distance (src/main.c:48-51: L = CPML dh, d0 = -3 ln R / (2 L), in T)
+        const T L = cfg.cpml * (T)cfg.dh;
+        const T d0 = (T)(-3 * log((double)cfg.r_coef) / (double)(2 * L));
+        k_cpml_table<T><<<(cfg.cpml + 128) / 128, 128, 0, st>>>(cpa, cpb, cfg.cpml, (T)cfg.vmax, (T)cfg.dt,
+                                                                 (T)cfg.dh, (T)cfg.f_cpml, d0, L);
+        TRY_LAUNCH();
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int copy_model_in(T *dst, const void *src)
+    {
+        TRY(cudaMemcpy2DAsync(dst, mpitch * sizeof(T), src, nx * sizeof(T), nx * sizeof(T), nz,
+                              cudaMemcpyDefault, st));
+        return FWI_OK;
+    }
+
+    int set_model(const void *a, const void *b, const void *c) override
+    {
+        if (!a || !b || !c) return FWI_ERR_ARG;
+        int rc;
+        if ((rc = copy_model_in(vh, a)) || (rc = copy_model_in(vp, b)) || (rc = copy_model_in(vn, c))) return rc;
+        have_model = true;
+        models_dirty = true;
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int set_model_vti(const void *vel, const void *eps, const void *del) override
+    {
+        if (!vel || !eps || !del) return FWI_ERR_ARG;
+        // stage the three inputs in the gradient buffers (free here), then transform
+        const size_t bytes = (size_t)nx * nz * sizeof(T);
+        TRY(cudaMemcpyAsync(grad[0], vel, bytes, cudaMemcpyDefault, st));
+        TRY(cudaMemcpyAsync(grad[1], eps, bytes, cudaMemcpyDefault, st));
+        TRY(cudaMemcpyAsync(grad[2], del, bytes, cudaMemcpyDefault, st));
+        k_pre_variables<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(grad[0], grad[1], grad[2], vh, vp, vn, nx,
+                                                                     nz, mpitch);
+        TRY_LAUNCH();
+        launches++;
+        have_model = true;
+        have_grad = false;
+        models_dirty = true;
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int get_model(void *a, void *b, void *c) override
+    {
+        T *src[3] = {vh, vp, vn};
+        void *dst[3] = {a, b, c};
+        for (int k = 0; k < 3; k++)
+            if (dst[k])
+                TRY(cudaMemcpy2DAsync(dst[k], nx * sizeof(T), src[k], mpitch * sizeof(T), nx * sizeof(T), nz,
+                                      cudaMemcpyDefault, st));
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int set_wavelet(const void *w, int nt) override
+    {
+        if (!w || nt <= 0 || nt > nt_max) return FWI_ERR_ARG;
+        TRY(cudaMemsetAsync(wavelet, 0, nt_max * sizeof(T), st));
+        TRY(cudaMemcpyAsync(wavelet, w, nt * sizeof(T), cudaMemcpyDefault, st));
+        TRY(cudaStreamSynchronize(st));
+        have_wavelet = true;
+        wavelet_nt = nt;
+        return FWI_OK;
+    }
+
+    int set_ricker(float f, int nt) override
+    {
+        if (nt <= 0 || nt > nt_max || !(f > 0)) return FWI_ERR_ARG;
+        // src/main.c:328-332 (host setup of the source, FP32 time accumulation)
+        std::vector<T> w(nt);
+        float t = 0;
+        for (int it = 0; it < nt; it++) {
+            t += cfg.dt;
+            double a = 3.141592653589793 * f * (t - (1 / f));
+            w[it] = (T)(1 * (1 - 2 * pow(a, 2)) * exp(-pow(a, 2)));
+        }
+        return set_wavelet(w.data(), nt);
+    }
+
+    int refresh_models()
+    {
+        if (!models_dirty) return FWI_OK;
+        const T dt2 = (T)cfg.dt * (T)cfg.dt;
+        k_scale_models<T><<<elt_grid(mslot), 256, 0, st>>>(vh, vp, vn, mh, mp, mn, dt2, mslot);
+        TRY_LAUNCH();
+        launches++;
+        models_dirty = false;
+        return FWI_OK;
+    }
+
+    int check_shot(const fwi_shot &s, DevShot &d) const
+    {
+        const int x0 = s.nxw > 0 ? s.x0 : 0;
+        const int w = s.nxw > 0 ? s.nxw : nx;
+        if (x0 < 0 || x0 + w > nx || w > (cfg.max_window > 0 ? cfg.max_window : nx)) return FWI_ERR_ARG;
+        if (w < 2 * cfg.cpml + 9 || nz < cfg.cpml + 9) return FWI_ERR_ARG;
+        if (s.nt <= 0 || s.nt > nt_max || s.nt > wavelet_nt) return FWI_ERR_ARG;
+        const int lsx = s.sx - x0, lr0 = s.rx0 - x0, lr1 = s.rx1 - x0;
+        if (!fwi::interior(lsx, s.sz, w, nz)) return FWI_ERR_ARG;
+        if (lr1 <= lr0 || lr1 - lr0 > nrec_max) return FWI_ERR_ARG;
+        if (!fwi::interior(lr0, s.rz, w, nz) || !fwi::interior(lr1 - 1, s.rz, w, nz)) return FWI_ERR_ARG;
+        d.x0 = x0; d.nx = w; d.sx = lsx; d.sz = s.sz; d.rz = s.rz; d.rx0 = lr0; d.rx1 = lr1; d.nt = s.nt;
+        d.rec_off = 0;
+        return FWI_OK;
+    }
+
+    Batch<T> batch_view(int nb) const
+    {
+        Batch<T> b;
+        b.B = nb; b.nz = nz; b.pitch = pitch; b.mpitch = mpitch; b.cpml = cfg.cpml; b.nt_max = nt_max;
+        b.slot = slot;
+        for (int k = 0; k < 4; k++) b.lvl[k] = lvl[k];
+        for (int k = 0; k < 8; k++) b.cp[k] = cp[k];
+        for (int k = 0; k < 3; k++) b.g[k] = gs[k];
+        b.store = store; b.store_type = store_type(); b.n_img = n_img;
+        b.scale = scale; b.amax = amax; b.rec = rec; b.shots = shots;
+        b.mh = mh; b.mp = mp; b.mn = mn; b.cpa = cpa; b.cpb = cpb; b.wavelet = wavelet;
+        b.inv_dh = T(1) / (T)cfg.dh;
+        b.inv_dh2 = T(1) / ((T)cfg.dh * (T)cfg.dh);
+        b.img_scale = cfg.mode == FWI_MODE_EXACT ? (T)cfg.dt * (T)cfg.dt : (T)cfg.dt;
+        b.status = status;
+        return b;
+    }
+
+    // Forward (+ residual + adjoint) of all shots, batch by batch.
+    int run(const fwi_shot *sh, int n, const void *obs_in, const unsigned char *mask_in, void *o_h, void *o_p,
+            void *o_n, double *misfit_out, void *traces, bool want_grad) override
+    {
+        if (!have_model || !have_wavelet) return FWI_ERR_STATE;
+        if (!sh || n <= 0) return FWI_ERR_ARG;
+        if ((want_grad || misfit_out) && !obs_in) return FWI_ERR_ARG;
+        std::vector<DevShot> all(n);
+        std::vector<long> off(n + 1, 0), moff(n + 1, 0);
+        for (int k = 0; k < n; k++) {
+            int rc = check_shot(sh[k], all[k]);
+            if (rc) return rc;
+            off[k + 1] = off[k] + (long)all[k].nt * (all[k].rx1 - all[k].rx0);
+            moff[k + 1] = moff[k] + (all[k].rx1 - all[k].rx0);
+        }
+        const bool exact = cfg.mode == FWI_MODE_EXACT;
+        int rc = refresh_models();
+        if (rc) return rc;
+        TRY(cudaEventRecord(ev[0], st));
+        long launches0 = launches;
+        if (want_grad)
+            for (auto &p : grad) TRY(cudaMemsetAsync(p, 0, mslot * sizeof(T), st));
+        TRY(cudaMemsetAsync(misfit, 0, sizeof(double), st));
+        TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+        float t_fwd = 0, t_adj = 0;
+        for (int b0 = 0; b0 < n; b0 += B) {
+            const int nb = std::min(B, n - b0);
+            int ntb = 0, nxm = 0;
+            std::vector<DevShot> bs(all.begin() + b0, all.begin() + b0 + nb);
+            std::vector<long> bmo(nb);
+            for (int k = 0; k < nb; k++) {
+                bs[k].rec_off = off[b0 + k] - off[b0];
+                bmo[k] = moff[b0 + k] - moff[b0];
+                ntb = std::max(ntb, bs[k].nt);
+                nxm = std::max(nxm, bs[k].nx);
+            }
+            const long nrec_elems = off[b0 + nb] - off[b0];
+            TRY(cudaMemcpyAsync(shots, bs.data(), nb * sizeof(DevShot), cudaMemcpyHostToDevice, st));
+            TRY(cudaMemcpyAsync(mask_off, bmo.data(), nb * sizeof(long), cudaMemcpyHostToDevice, st));
+            if (obs_in)
+                TRY(cudaMemcpyAsync(obs, (const T *)obs_in + off[b0], nrec_elems * sizeof(T), cudaMemcpyDefault, st));
+            if (mask_in)
+                TRY(cudaMemcpyAsync(mask, mask_in + moff[b0], moff[b0 + nb] - moff[b0], cudaMemcpyDefault, st));
+            const size_t lb = (size_t)nb * slot * sizeof(T);
+            for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+            for (int k = 0; k < 4; k++) TRY(cudaMemsetAsync(cp[k], 0, lb, st));
+            TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
+            Batch<T> b = batch_view(nb);
+            cudaEvent_t e0 = ev[1], e1 = ev[2], e2 = ev[3];
+            TRY(cudaEventRecord(e0, st));
+            int cur = 0;
+            for (int g = 0; g < ntb; g++) {
+                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, want_grad ? g : -1, exact, st);
+                cur ^= 1;
+            }
+            TRY_LAUNCH();
+            launches += 2L * ntb;
+            TRY(cudaEventRecord(e1, st));
+            if (obs_in) {
+                k_residual<T><<<dim3(kRedBlocks, nb), kRedThreads, 0, st>>>(rec, obs, mask_in ? mask : nullptr, shots,
+                                                                          mask_off, partial);
+                k_misfit_finish<<<1, 256, 0, st>>>(partial, (long)nb * kRedBlocks, misfit);
+                TRY_LAUNCH();
+                launches += 2;
+            }
+            if (traces)
+                TRY(cudaMemcpyAsync((T *)traces + off[b0], rec, nrec_elems * sizeof(T), cudaMemcpyDefault, st));
+            if (want_grad) {
+                for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+                for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
+                for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
+                cur = 0;
+                int zsel = 0;
+                for (int j = 0; j < ntb; j++) {
+                    fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, st);
+                    cur ^= 1;
+                    zsel ^= 1;
+                }
+                TRY_LAUNCH();
+                launches += 2L * ntb;
+                k_accumulate_gradient<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(
+                    grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, nb, nx, nz, mpitch, pitch, slot);
+                TRY_LAUNCH();
+                launches++;
+            }
+            TRY(cudaEventRecord(e2, st));
+            TRY(cudaEventSynchronize(e2));
+            float a = 0, c = 0;
+            cudaEventElapsedTime(&a, e0, e1);
+            cudaEventElapsedTime(&c, e1, e2);
+            t_fwd += a;
+            t_adj += c;
+        }
+        unsigned stat = 0;
+        TRY(cudaMemcpyAsync(&stat, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        if (misfit_out) TRY(cudaMemcpyAsync(misfit_out, misfit, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (want_grad) {
+            void *outs[3] = {o_h, o_p, o_n};
+            for (int k = 0; k < 3; k++)
+                if (outs[k])
+                    TRY(cudaMemcpy2DAsync(outs[k], nx * sizeof(T), grad[k], mpitch * sizeof(T), nx * sizeof(T), nz,
+                                          cudaMemcpyDefault, st));
+            have_grad = true;
+        }
+        cudaEvent_t eend;
+        TRY(cudaEventCreate(&eend));
+        cudaEventRecord(eend, st);
+        cudaError_t se = cudaEventSynchronize(eend);
+        float tot = 0;
+        cudaEventElapsedTime(&tot, ev[0], eend);
+        cudaEventDestroy(eend);
+        TRY(se);
+        timing[0] = tot;
+        timing[1] = t_fwd;
+        timing[2] = t_adj;
+        timing[3] = tot - t_fwd - t_adj;
+        launches = launches - launches0;
+        if (stat & 1u) return FWI_ERR_NUMERIC;
+        if (misfit_out && !std::isfinite(*misfit_out)) return FWI_ERR_NUMERIC;
+        return FWI_OK;
+    }
+
+    // ---------------------------------------------------------------- L-BFGS
+
+    Tri<T> tri(T *const (&a)[3]) const { Tri<T> t; for (int k = 0; k < 3; k++) t.p[k] = a[k]; return t; }
+    CTri<T> ctri(T *const (&a)[3]) const { CTri<T> t; for (int k = 0; k < 3; k++) t.p[k] = a[k]; return t; }
+    CTri<T> cnull() const { CTri<T> t; for (int k = 0; k < 3; k++) t.p[k] = nullptr; return t; }
+
+    int copy3(T *const (&dst)[3], T *const (&src)[3])
+    {
+        for (int k = 0; k < 3; k++) TRY(cudaMemcpyAsync(dst[k], src[k], mslot * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        return FWI_OK;
+    }
+
+    int first_step(float a_hor, float a_po, float a_nmo) override
+    {
+        if (!have_grad || !have_model) return FWI_ERR_STATE;
+        T *m3[3] = {vh, vp, vn};
+        int rc;
+        if ((rc = copy3(mb, m3)) || (rc = copy3(gb, grad))) return rc;
+        have_back = true;
+        // |g|^2 over the whole grid (src/main.c:551-559), in FP64
+        k_lb_copy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(q), ctri(grad), ctri(grad), mslot, ds, lbs->dots);
+        k_lb_inv_norm<<<1, 32, 0, st>>>(lbs);
+        k_first_update<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(vh, vp, vn, grad[0], grad[1], grad[2], lbs, a_hor,
+                                                                   a_po, a_nmo, nx, nz, mpitch);
+        TRY_LAUNCH();
+        launches += 3;
+        models_dirty = true;
+        hist_count = 0;
+        hist_next = 0;
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int ensure_history(int m)
+    {
+        if (m <= hist_m) return FWI_OK;
+        for (int l = hist_m; l < m; l++)
+            for (int p = 0; p < 3; p++) {
+                TRY(alloc(&hs[l][p], mslot));
+                TRY(alloc(&hy[l][p], mslot));
+            }
+        hist_m = m;
+        return FWI_OK;
+    }
+
+    int lbfgs_direction(int m, double *stats) override
+    {
+        if (m < 1 || m > kMaxHist) return FWI_ERR_ARG;
+        if (!have_grad || !have_back) return FWI_ERR_STATE;
+        int rc = ensure_history(m);
+        if (rc) return rc;
+        if (hist_count > m) hist_count = m;
+        // newest pair into the ring
+        const int k = hist_next % m;
+        T *sk[3] = {hs[k][0], hs[k][1], hs[k][2]}, *yk[3] = {hy[k][0], hy[k][1], hy[k][2]};
+        T *m3[3] = {vh, vp, vn};
+        k_lb_pair<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(sk), tri(yk), ctri(m3), ctri(mb), ctri(grad), ctri(gb),
+                                                         mslot, ds, lbs->pair);
+        hist_next = (hist_next + 1) % m;
+        hist_count = std::min(hist_count + 1, m);
+        // order newest .. oldest
+        std::vector<int> order;
+        for (int a = 0; a < hist_count; a++) order.push_back(((hist_next - 1 - a) % m + m) % m);
+        // first loop; q = g and rho_k, alpha_k of the newest pair
+        int rcq = copy3(q, grad);
+        if (rcq) return rcq;
+        k_lb_scalar<<<1, 32, 0, st>>>(lbs, 0, order[0]);
+        // rho of the older slots persists from when they were formed
+        for (size_t a = 0; a < order.size(); a++) {
+            const int l = order[a];
+            T *yl[3] = {hy[l][0], hy[l][1], hy[l][2]};
+            if (a > 0) k_lb_scalar<<<1, 32, 0, st>>>(lbs, 1, l);
+            const bool has_next = a + 1 < order.size();
+            const int ln = has_next ? order[a + 1] : l;
+            T *sn[3] = {hs[ln][0], hs[ln][1], hs[ln][2]};
+            k_lb_axpy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(q), ctri(yl), nullptr, lbs->coefB, ctri(sn),
+                                                                 has_next ? 1 : 0, mslot, ds, lbs->dots);
+        }
+        // r = gamma q; then the second loop oldest .. newest
+        k_lb_scalar<<<1, 32, 0, st>>>(lbs, 2, 0);
+        int first = order.back();
+        T *y0[3] = {hy[first][0], hy[first][1], hy[first][2]};
+        rcq = copy3(r, q);
+        if (rcq) return rcq;
+        k_lb_axpy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(r), cnull(), lbs->coefA, nullptr, ctri(y0), 1, mslot,
+                                                             ds, lbs->dots);
+        for (int a = (int)order.size() - 1; a >= 0; a--) {
+            const int l = order[a];
+            T *sl[3] = {hs[l][0], hs[l][1], hs[l][2]};
+            k_lb_scalar<<<1, 32, 0, st>>>(lbs, 3, l);
+            const bool has_next = a > 0;
+            const int ln = has_next ? order[a - 1] : l;
+            T *yn[3] = {hy[ln][0], hy[ln][1], hy[ln][2]};
+            k_lb_axpy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(r), ctri(sl), nullptr, lbs->coefB, ctri(yn),
+                                                                 has_next ? 1 : 0, mslot, ds, lbs->dots);
+        }
+        TRY_LAUNCH();
+        // the model and gradient this direction starts from (src/main.c:683-688)
+        if ((rc = copy3(mb, m3)) || (rc = copy3(gb, grad))) return rc;
+        if (stats) {
+            LbScalars h;
+            TRY(cudaMemcpyAsync(&h, lbs, sizeof(h), cudaMemcpyDeviceToHost, st));
+            TRY(cudaStreamSynchronize(st));
+            for (int p = 0; p < 3; p++) {
+                stats[p] = h.gamma[p];
+                stats[3 + p] = h.rho[p][order[0]];
+                stats[6 + p] = h.pair[p];      // y.s of the newest pair
+                stats[9 + p] = h.pair[3 + p];  // y.y of the newest pair
+            }
+        }
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int lbfgs_update(float av, float ad, float ae, int fmin, int fmax) override
+    {
+        if (!have_back) return FWI_ERR_STATE;
+        // av, ad, ae pair with (v_po, v_nmo, v_hor) as update_LBFGS does (src/main.c:693)
+        k_lb_update<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(vh, vp, vn, mb[0], mb[1], mb[2], r[0], r[1], r[2], av,
+                                                                ad, ae, fmin, fmax, nx, nz, mpitch);
+        TRY_LAUNCH();
+        launches++;
+        models_dirty = true;
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int restore_model() override
+    {
+        if (!have_back) return FWI_ERR_STATE;
+        T *m3[3] = {vh, vp, vn};
+        int rc = copy3(m3, mb);
+        if (rc) return rc;
+        models_dirty = true;
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int set_gradient(const void *a, const void *b, const void *c) override
+    {
+        if (!a || !b || !c) return FWI_ERR_ARG;
+        int rc;
+        if ((rc = copy_model_in(grad[0], a)) || (rc = copy_model_in(grad[1], b)) || (rc = copy_model_in(grad[2], c)))
+            return rc;
+        TRY(cudaStreamSynchronize(st));
+        have_grad = true;
+        return FWI_OK;
+    }
+
+    int gradient_vti(void *o0, void *o1, void *o2) override
+    {
+        if (!have_grad) return FWI_ERR_STATE;
+        for (auto &p : vti_out)
+            if (!p) TRY(alloc(&p, mslot));
+        k_grad_vti<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(vh, vp, vn, grad[0], grad[1], grad[2], vti_out[0],
+                                                               vti_out[1], vti_out[2], nx, nz, mpitch);
+        TRY_LAUNCH();
+        void *outs[3] = {o0, o1, o2};
+        for (int k = 0; k < 3; k++)
+            if (outs[k])
+                TRY(cudaMemcpy2DAsync(outs[k], nx * sizeof(T), vti_out[k], mpitch * sizeof(T), nx * sizeof(T), nz,
+                                      cudaMemcpyDefault, st));
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+};
+
+CtxBase *as_ctx(void *p) { return static_cast<CtxBase *>(p); }
+
+}  // namespace
+
+extern "C" {
+
+void fwi_config_default(fwi_config *c)
+{
+    if (!c) return;
+    memset(c, 0, sizeof(*c));
+    c->nx = 201;
+    c->nz = 201;
+    c->dh = 10.f;
+    c->dt = 1e-3f;
+    c->cpml = 20;
+    c->f_cpml = 10.f;
+    c->vmax = 6000.f;
+    c->r_coef = 1e-6f;
+    c->nt_max = 2000;
+    c->max_shots = 1;
+    c->mode = FWI_MODE_EXACT;
+    c->precision = FWI_PREC_FP32;
+    c->store = FWI_STORE_FULL;
+    c->store_prec = FWI_SPREC_NATIVE;
+}
+
+size_t fwi_config_bytes(const fwi_config *c)
+{
+    if (!c) return 0;
+    const size_t e = c->precision == FWI_PREC_FP64 ? 8 : 4;
+    const size_t se = c->store_prec == FWI_SPREC_NATIVE ? e : 2;
+    const long win = c->max_window > 0 ? c->max_window : c->nx;
+    const long slot = (long)c->nz * round_up(win, 32), mslot = (long)c->nz * round_up(c->nx, 32);
+    const long nrec = c->max_receivers > 0 ? c->max_receivers : win;
+    size_t b = 0;
+    b += (size_t)(6 + 3 + 12) * mslot * e;                 // models, gradient, L-BFGS work arrays
+    b += (size_t)c->max_shots * slot * e * (4 + 8 + 3);    // levels, CPML state, per-shot gradients
+    b += (size_t)c->max_shots * c->nt_max * 2 * slot * se; // images
+    b += (size_t)c->max_shots * c->nt_max * nrec * e * 2;  // records and observed data
+    return b;
+}
+
+int fwi_create(const fwi_config *cfg, void **out)
+{
+    if (!cfg || !out) return FWI_ERR_ARG;
+    *out = nullptr;
+    if (cfg->nx < 2 * cfg->cpml + 9 || cfg->nz < cfg->cpml + 9 || cfg->cpml < 0 || cfg->nt_max <= 0 ||
+        cfg->max_shots <= 0 || !(cfg->dh > 0) || !(cfg->dt > 0) || cfg->max_window < 0 || cfg->max_window > cfg->nx)
+        return FWI_ERR_ARG;
+    if (cfg->mode != FWI_MODE_EXACT && cfg->mode != FWI_MODE_REF_COMPAT) return FWI_ERR_ARG;
+    if (cfg->store != FWI_STORE_FULL) return FWI_ERR_UNSUPPORTED;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device) {
+        cudaGetLastError();
+        return FWI_ERR_NODEVICE;
+    }
+    CtxBase *c = nullptr;
+    if (cfg->precision == FWI_PREC_FP32) c = new Ctx<float>();
+    else if (cfg->precision == FWI_PREC_FP64) c = new Ctx<double>();
+    else return FWI_ERR_ARG;
+    c->cfg = *cfg;
+    int rc = c->init();
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return FWI_OK;
+}
+
+void fwi_destroy(void *ctx) { delete as_ctx(ctx); }
+
+const char *fwi_strerror(int s)
+{
+    switch (s) {
+    case FWI_OK: return "ok";
+    case FWI_ERR_ARG: return "invalid argument";
+    case FWI_ERR_CUDA: return "CUDA error";
+    case FWI_ERR_NOMEM: return "out of device memory";
+    case FWI_ERR_STATE: return "call out of order";
+    case FWI_ERR_NUMERIC: return "non-finite value or saturated image storage";
+    case FWI_ERR_UNSUPPORTED: return "unsupported configuration";
+    case FWI_ERR_NODEVICE: return "no usable CUDA device";
+    default: return "unknown status";
+    }
+}
+
+int fwi_last_cuda_error(void *ctx) { return ctx ? as_ctx(ctx)->last_cuda : 0; }
+
+int fwi_set_model(void *ctx, const void *a, const void *b, const void *c)
+{
+    return ctx ? as_ctx(ctx)->set_model(a, b, c) : FWI_ERR_ARG;
+}
+int fwi_set_model_vti(void *ctx, const void *a, const void *b, const void *c)
+{
+    return ctx ? as_ctx(ctx)->set_model_vti(a, b, c) : FWI_ERR_ARG;
+}
+int fwi_get_model(void *ctx, void *a, void *b, void *c) { return ctx ? as_ctx(ctx)->get_model(a, b, c) : FWI_ERR_ARG; }
+int fwi_set_wavelet(void *ctx, const void *w, int nt) { return ctx ? as_ctx(ctx)->set_wavelet(w, nt) : FWI_ERR_ARG; }
+int fwi_set_ricker(void *ctx, float f, int nt) { return ctx ? as_ctx(ctx)->set_ricker(f, nt) : FWI_ERR_ARG; }
+
+int fwi_forward(void *ctx, const fwi_shot *shots, int n, void *traces)
+{
+    if (!ctx || !traces) return FWI_ERR_ARG;
+    return as_ctx(ctx)->run(shots, n, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, traces, false);
+}
+
+int fwi_gradient(void *ctx, const fwi_shot *shots, int n, const void *obs, const unsigned char *mask, void *gh,
+                 void *gp, void *gn, double *misfit)
+{
+    if (!ctx) return FWI_ERR_ARG;
+    return as_ctx(ctx)->run(shots, n, obs, mask, gh, gp, gn, misfit, nullptr, true);
+}
+
+int fwi_misfit(void *ctx, const fwi_shot *shots, int n, const void *obs, const unsigned char *mask, double *misfit)
+{
+    if (!ctx || !misfit) return FWI_ERR_ARG;
+    return as_ctx(ctx)->run(shots, n, obs, mask, nullptr, nullptr, nullptr, misfit, nullptr, false);
+}
+
+int fwi_set_gradient(void *ctx, const void *a, const void *b, const void *c)
+{
+    return ctx ? as_ctx(ctx)->set_gradient(a, b, c) : FWI_ERR_ARG;
+}
+int fwi_first_step(void *ctx, float a, float b, float c) { return ctx ? as_ctx(ctx)->first_step(a, b, c) : FWI_ERR_ARG; }
+int fwi_lbfgs_direction(void *ctx, int m, double *stats)
+{
+    return ctx ? as_ctx(ctx)->lbfgs_direction(m, stats) : FWI_ERR_ARG;
+}
+int fwi_lbfgs_update(void *ctx, float av, float ad, float ae, int fmin, int fmax)
+{
+    return ctx ? as_ctx(ctx)->lbfgs_update(av, ad, ae, fmin, fmax) : FWI_ERR_ARG;
+}
+int fwi_restore_model(void *ctx) { return ctx ? as_ctx(ctx)->restore_model() : FWI_ERR_ARG; }
+int fwi_gradient_vti(void *ctx, void *a, void *b, void *c) { return ctx ? as_ctx(ctx)->gradient_vti(a, b, c) : FWI_ERR_ARG; }
+
+int fwi_last_timing(void *ctx, float *out4)
+{
+    if (!ctx || !out4) return FWI_ERR_ARG;
+    memcpy(out4, as_ctx(ctx)->timing, sizeof(float) * 4);
+    return FWI_OK;
+}
+
+long fwi_last_launches(void *ctx) { return ctx ? as_ctx(ctx)->launches : 0; }
+
+long fwi_strip_points(int nx, int nz, int cpml, int *ix, int *iz, long cap)
+{
+    fwi::StripMap sm = fwi::StripMap::make(nx, nz, cpml);
+    long n = sm.count();
+    for (long k = 0; k < n && k < cap; k++) {
+        int a, b;
+        sm.point(k, a, b);
+        if (ix) ix[k] = a;
+        if (iz) iz[k] = b;
+    }
+    return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,66 @@
+// Internal interface between the native context (native.cu) and the batched
+// propagation kernels (prop.cuh, instantiated in prop_f32.cu / prop_f64.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace fwi {
+
+// One shot of a batch, in the shot's own window coordinates.
+struct DevShot {
+    int x0;        // first model column of the window
+    int nx;        // window width (the shot's grid nx)
+    int sx, sz;    // source point
+    int rz, rx0, rx1;  // receiver row and columns [rx0, rx1)
+    int nt;        // time steps
+    long rec_off;  // offset of this shot's [nt][nrec] record / residual / observed block
+};
+
+enum StoreType { kStoreNative = 0, kStoreHalf = 1, kStoreBf16 = 2 };
+
+// Device buffers of one batch of up to B shots.  Per-shot arrays are
+// [B][nz][pitch] (slot = nz * pitch elements per shot).
+template <typename T> struct Batch {
+    int B, nz, pitch, mpitch, cpml, nt_max;
+    long slot;
+    T *lvl[4];      // P level 0, P level 1, F level 0, F level 1
+    T *cp[8];       // CPML memory variables (forward uses 0..3)
+    T *g[3];        // per-shot gradient accumulators: v_hor, v_po, v_nmo
+    void *store;    // images: [B][n_img][2][slot] of the store type
+    int store_type; // StoreType
+    int n_img;      // image slots per shot
+    float *scale;   // [B][nt_max] encode scale of each stored image step
+    float *amax;    // [B][nt_max + 1] max |P|, |F| after each step
+    T *rec;         // records / residuals, at DevShot::rec_off
+    const DevShot *shots;
+    const T *mh, *mp, *mn;  // dt^2 v_hor, dt^2 v_po, dt^2 v_nmo, [nz][mpitch]
+    const T *cpa, *cpb;     // CPML a, b by distance into the layer [cpml + 1]
+    const T *wavelet;
+    T inv_dh, inv_dh2;
+    T img_scale;            // dt (reference imaging) or dt^2 (exact)
+    unsigned *status;       // bit 0: stored image saturated
+};
+
+// Shots of a batch run end-aligned on one global clock of `ntb` steps (the
+// batch's longest shot): shot s does its local step it = g - (ntb - nt_s),
+// so every shot's adjoint starts at the same global iteration and the image
+// a given adjoint iteration needs sits at the same global step for all shots.
+
+// Forward global step g.  `cur` is the level holding each shot's current
+// state; the new state overwrites level 1 - cur.  With img_slot >= 0 the
+// step's images go to that slot (G, H for exact imaging, Dxx P and Dzz F for
+// the reference's).  Receiver traces are always recorded.
+template <typename T>
+void launch_forward_step(const Batch<T> &b, int nx_max, int g, int ntb, int cur, int img_slot,
+                         bool exact, cudaStream_t st);
+
+// Adjoint iteration j: lambda^m, m = nt_s - j, of every shot with nt_s > j.
+// `cur` holds lambda^{m+1}; lambda^m overwrites level 1 - cur.  `zsel`
+// selects the ping-pong half of the exact adjoint's Z state.  The image of
+// global step ntb - 1 - lag - j (lag 0 exact, 1 reference) is read from slot
+// (that step - img_base); img_base <= that step is the caller's contract.
+template <typename T>
+void launch_adjoint_step(const Batch<T> &b, int nx_max, int j, int ntb, int cur, int zsel,
+                         bool exact, int img_base, cudaStream_t st);
+
+}  // namespace fwi

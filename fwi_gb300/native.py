@@ -1,0 +1,280 @@
+"""ctypes bindings of libfwi_gb300.so: the native ABI (include/fwi.h) and the
+reference-compatible ABI (include/fwi_compat.h).
+
+Array arguments are anything exposing a data pointer: numpy arrays (host) or
+torch tensors (host or CUDA; `data_ptr()`).  The library detects host versus
+device memory per call.  There is no fallback: if the shared library is not
+built, `lib()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libfwi_gb300.so")
+
+FWI_OK = 0
+FWI_ERR_ARG = -1
+FWI_ERR_CUDA = -2
+FWI_ERR_NOMEM = -3
+FWI_ERR_STATE = -4
+FWI_ERR_NUMERIC = -5
+FWI_ERR_UNSUPPORTED = -6
+FWI_ERR_NODEVICE = -7
+
+MODE_REF_COMPAT, MODE_EXACT = 0, 1
+PREC_FP32, PREC_FP64 = 0, 1
+STORE_FULL, STORE_CHECKPOINT = 0, 1
+SPREC_NATIVE, SPREC_FP16, SPREC_BF16 = 0, 1, 2
+
+COMPAT_SYMBOLS = [
+    "pre_variables_h", "CPML_x_h", "CPML_z_h", "PSI_F_h", "ZETA_F_h", "propagator_F_h", "res_h",
+    "SecondDerivate_P_h", "launchPropagation", "launchBackPropagation", "NORMAL_h", "UpdateModel_h",
+    "compute_sy_h", "compute_qi_h", "compute_ri_h", "update_r_h", "update_LBFGS_h",
+]
+
+
+class FwiError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        msg = lib().fwi_strerror(status).decode() if _LIB is not None else str(status)
+        super().__init__(f"{what}: {msg} ({status})")
+
+
+class Config(C.Structure):
+    _fields_ = [("nx", C.c_int), ("nz", C.c_int), ("dh", C.c_float), ("dt", C.c_float),
+                ("cpml", C.c_int), ("f_cpml", C.c_float), ("vmax", C.c_float), ("r_coef", C.c_float),
+                ("nt_max", C.c_int), ("max_shots", C.c_int), ("max_window", C.c_int),
+                ("max_receivers", C.c_int), ("mode", C.c_int), ("precision", C.c_int),
+                ("store", C.c_int), ("store_prec", C.c_int), ("ckpt_every", C.c_int),
+                ("device", C.c_int)]
+
+
+class Shot(C.Structure):
+    _fields_ = [("sx", C.c_int), ("sz", C.c_int), ("rz", C.c_int), ("rx0", C.c_int),
+                ("rx1", C.c_int), ("nt", C.c_int), ("x0", C.c_int), ("nxw", C.c_int)]
+
+    @property
+    def nrec(self):
+        return self.rx1 - self.rx0
+
+
+_LIB = None
+_p, _i, _f, _d, _l = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_long
+
+
+def _sig(L, name, args, res=_i):
+    fn = getattr(L, name)
+    fn.argtypes = args
+    fn.restype = res
+
+
+def lib() -> C.CDLL:
+    """Load the library (built by fwi_gb300.build / __graft_entry__.build)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is not built; run `python -m fwi_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        cfgp, shotp = C.POINTER(Config), C.POINTER(Shot)
+        _sig(L, "fwi_config_default", [cfgp], None)
+        _sig(L, "fwi_config_bytes", [cfgp], C.c_size_t)
+        _sig(L, "fwi_create", [cfgp, C.POINTER(_p)])
+        _sig(L, "fwi_destroy", [_p], None)
+        _sig(L, "fwi_strerror", [_i], C.c_char_p)
+        _sig(L, "fwi_last_cuda_error", [_p])
+        _sig(L, "fwi_set_model", [_p, _p, _p, _p])
+        _sig(L, "fwi_set_model_vti", [_p, _p, _p, _p])
+        _sig(L, "fwi_get_model", [_p, _p, _p, _p])
+        _sig(L, "fwi_set_wavelet", [_p, _p, _i])
+        _sig(L, "fwi_set_ricker", [_p, _f, _i])
+        _sig(L, "fwi_forward", [_p, shotp, _i, _p])
+        _sig(L, "fwi_gradient", [_p, shotp, _i, _p, _p, _p, _p, _p, C.POINTER(_d)])
+        _sig(L, "fwi_misfit", [_p, shotp, _i, _p, _p, C.POINTER(_d)])
+        _sig(L, "fwi_set_gradient", [_p, _p, _p, _p])
+        _sig(L, "fwi_first_step", [_p, _f, _f, _f])
+        _sig(L, "fwi_lbfgs_direction", [_p, _i, _p])
+        _sig(L, "fwi_lbfgs_update", [_p, _f, _f, _f, _i, _i])
+        _sig(L, "fwi_restore_model", [_p])
+        _sig(L, "fwi_gradient_vti", [_p, _p, _p, _p])
+        _sig(L, "fwi_last_timing", [_p, _p])
+        _sig(L, "fwi_last_launches", [_p], _l)
+        _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
+        # reference-compatible ABI: float* device pointers, ints, floats
+        _sig(L, "pre_variables_h", [_p] * 6 + [_i, _i], None)
+        _sig(L, "CPML_x_h", [_p, _p, _i, _f, _i, _f, _f, _f, _f, _f], None)
+        _sig(L, "CPML_z_h", [_p, _p, _i, _f, _i, _f, _f, _f, _f, _f], None)
+        _sig(L, "PSI_F_h", [_p] * 8 + [_i, _i, _f, _i], None)
+        _sig(L, "ZETA_F_h", [_p] * 14 + [_i, _i, _f, _f, _i], None)
+        _sig(L, "propagator_F_h", [_p] * 14 + [_f, _f] + [_i] * 6, None)
+        _sig(L, "res_h", [_p] * 3 + [_i, _i], None)
+        _sig(L, "SecondDerivate_P_h", [_p] * 4 + [_f, _i, _i], None)
+        _sig(L, "launchPropagation", [_p] * 10 + [_f, _i, _i] + [_p] * 6 + [_f, _i] + [_p] * 9 +
+             [_f, _i, _i, _i], None)
+        _sig(L, "launchBackPropagation", [_p, _p, _i, _i, _i] + [_p] * 16 + [_f] + [_p] * 10 +
+             [_f, _i] + [_p] * 9 + [_f, _p, _i, _i, _i, _f, _p, _p, _p], None)
+        _sig(L, "NORMAL_h", [_p] * 3 + [_i, _i, _f, _f, _f], None)
+        _sig(L, "UpdateModel_h", [_p] * 6 + [_f, _f, _f, _i, _i], None)
+        _sig(L, "compute_sy_h", [_p] * 18 + [_i, _i, _i], None)
+        _sig(L, "compute_qi_h", [_p] * 6 + [_f, _f, _f, _i, _i, _i], None)
+        _sig(L, "compute_ri_h", [_p] * 6 + [_f, _f, _f, _i, _i], None)
+        _sig(L, "update_r_h", [_p] * 6 + [_f] * 6 + [_i, _i, _i], None)
+        _sig(L, "update_LBFGS_h", [_p] * 9 + [_i, _i, _f, _f, _f] + [_i] * 5, None)
+        _sig(L, "fwi_compat_last_error", [])
+        _LIB = L
+    return _LIB
+
+
+def ptr(x):
+    """Raw address of an array-like (numpy, torch) or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+        return x.ctypes.data
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def _check(status, what):
+    if status != FWI_OK:
+        raise FwiError(status, what)
+
+
+def make_shots(specs):
+    """Shot array from dicts / tuples (sx, sz, rz, rx0, rx1, nt[, x0, nxw])."""
+    arr = (Shot * len(specs))()
+    for k, s in enumerate(specs):
+        if isinstance(s, dict):
+            vals = [s.get(n, 0) for n, _ in Shot._fields_]
+        else:
+            vals = list(s) + [0] * (8 - len(s))
+        for (n, _), v in zip(Shot._fields_, vals):
+            setattr(arr[k], n, int(v))
+    return arr
+
+
+def strip_points(nx, nz, cpml):
+    """(ix, iz) of the CPML strip points, in the strip kernels' order (host only)."""
+    L = lib()
+    n = L.fwi_strip_points(nx, nz, cpml, None, None, 0)
+    ix = np.zeros(max(n, 1), np.int32)
+    iz = np.zeros(max(n, 1), np.int32)
+    L.fwi_strip_points(nx, nz, cpml, ix.ctypes.data, iz.ctypes.data, n)
+    return ix[:n], iz[:n]
+
+
+class Context:
+    """One native context (include/fwi.h)."""
+
+    def __init__(self, **kw):
+        L = lib()
+        cfg = Config()
+        L.fwi_config_default(C.byref(cfg))
+        for k, v in kw.items():
+            if not hasattr(cfg, k):
+                raise TypeError(f"unknown config field {k}")
+            setattr(cfg, k, v)
+        self.cfg = cfg
+        self.dtype = np.float64 if cfg.precision == PREC_FP64 else np.float32
+        h = _p()
+        _check(L.fwi_create(C.byref(cfg), C.byref(h)), "fwi_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fwi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_model(self, vh, vp, vn):
+        _check(lib().fwi_set_model(self._h, ptr(vh), ptr(vp), ptr(vn)), "fwi_set_model")
+
+    def set_model_vti(self, vel, eps, delta):
+        _check(lib().fwi_set_model_vti(self._h, ptr(vel), ptr(eps), ptr(delta)), "fwi_set_model_vti")
+
+    def get_model(self):
+        out = [np.zeros((self.cfg.nz, self.cfg.nx), self.dtype) for _ in range(3)]
+        _check(lib().fwi_get_model(self._h, *[ptr(o) for o in out]), "fwi_get_model")
+        return out
+
+    def set_wavelet(self, w):
+        w = np.ascontiguousarray(w, self.dtype) if isinstance(w, np.ndarray) else w
+        _check(lib().fwi_set_wavelet(self._h, ptr(w), len(w)), "fwi_set_wavelet")
+
+    def set_ricker(self, f, nt):
+        _check(lib().fwi_set_ricker(self._h, float(f), int(nt)), "fwi_set_ricker")
+
+    def forward(self, shots, out=None):
+        n = sum(s.nt * s.nrec for s in shots)
+        if out is None:
+            out = np.zeros(n, self.dtype)
+        _check(lib().fwi_forward(self._h, shots, len(shots), ptr(out)), "fwi_forward")
+        return out
+
+    def gradient(self, shots, obs, mask=None, out=None):
+        """Returns (misfit, g_vh, g_vp, g_vn); `out` may give three destination arrays."""
+        if out is None:
+            out = [np.zeros((self.cfg.nz, self.cfg.nx), self.dtype) for _ in range(3)]
+        J = C.c_double(0)
+        _check(lib().fwi_gradient(self._h, shots, len(shots), ptr(obs), ptr(mask),
+                                  *[ptr(o) for o in out], C.byref(J)), "fwi_gradient")
+        return (J.value, *out)
+
+    def misfit(self, shots, obs, mask=None):
+        J = C.c_double(0)
+        _check(lib().fwi_misfit(self._h, shots, len(shots), ptr(obs), ptr(mask), C.byref(J)),
+               "fwi_misfit")
+        return J.value
+
+    def set_gradient(self, gh, gp, gn):
+        _check(lib().fwi_set_gradient(self._h, ptr(gh), ptr(gp), ptr(gn)), "fwi_set_gradient")
+
+    def first_step(self, a_hor, a_po, a_nmo):
+        _check(lib().fwi_first_step(self._h, a_hor, a_po, a_nmo), "fwi_first_step")
+
+    def lbfgs_direction(self, m=5):
+        st = np.zeros(12, np.float64)
+        _check(lib().fwi_lbfgs_direction(self._h, m, st.ctypes.data), "fwi_lbfgs_direction")
+        return st
+
+    def lbfgs_update(self, av, ad, ae, flag_min=0, flag_max=0):
+        _check(lib().fwi_lbfgs_update(self._h, av, ad, ae, flag_min, flag_max), "fwi_lbfgs_update")
+
+    def restore_model(self):
+        _check(lib().fwi_restore_model(self._h), "fwi_restore_model")
+
+    def gradient_vti(self):
+        out = [np.zeros((self.cfg.nz, self.cfg.nx), self.dtype) for _ in range(3)]
+        _check(lib().fwi_gradient_vti(self._h, *[ptr(o) for o in out]), "fwi_gradient_vti")
+        return out
+
+    def last_timing(self):
+        t = np.zeros(4, np.float32)
+        _check(lib().fwi_last_timing(self._h, t.ctypes.data), "fwi_last_timing")
+        return t
+
+    def last_launches(self):
+        return int(lib().fwi_last_launches(self._h))

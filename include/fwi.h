@@ -1,0 +1,179 @@
+/*
+ * fwi.h -- native C-ABI of the GB300 (sm_103a) VTI FWI gradient library.
+ *
+ * One context owns every device buffer of the path.  Shots are a batch
+ * dimension: fwi_gradient() runs all shots of a call through one sequence of
+ * batched launches (forward, residual + misfit, adjoint + imaging, reduction)
+ * instead of the reference's one-shot-per-MPI-rank loop (src/main.c:408-496).
+ *
+ * Physics and grid are the reference's (src/parallelcalls.cu): 8th-order
+ * pseudo-acoustic VTI leapfrog on the coupled fields P, F; CPML on the left,
+ * right and bottom edges (none at the top); a 4-point zero frame on every
+ * edge; arrays [nz][nx], x fastest.  Models are the squared velocities
+ * v_hor = Vp^2 (1 + 2 eps), v_po = Vp^2, v_nmo = Vp^2 (1 + 2 delta).
+ *
+ * Element type of every array argument: float for FWI_PREC_FP32 contexts,
+ * double for FWI_PREC_FP64 contexts.  Pointers may be host or device memory
+ * (detected per call); host buffers are staged through the context.
+ *
+ * Every function returns FWI_OK (0) or a negative FWI_ERR_* status.
+ */
+#ifndef FWI_H
+#define FWI_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FWI_OK 0
+#define FWI_ERR_ARG (-1)       /* invalid argument or geometry */
+#define FWI_ERR_CUDA (-2)      /* a CUDA call failed (details: fwi_last_cuda_error) */
+#define FWI_ERR_NOMEM (-3)     /* device memory for the requested batch does not fit */
+#define FWI_ERR_STATE (-4)     /* call out of order (e.g. no model set) */
+#define FWI_ERR_NUMERIC (-5)   /* NaN/Inf met, or reduced-precision storage saturated */
+#define FWI_ERR_UNSUPPORTED (-6)
+#define FWI_ERR_NODEVICE (-7)  /* no CUDA device, or not an sm_103 device */
+
+/* Adjoint / imaging semantics of fwi_gradient(). */
+#define FWI_MODE_REF_COMPAT 0 /* the reference's gradient, src/main.c:408-496: its CPML adjoint
+                                 (src/parallelcalls.cu:179-243), forward image of the step
+                                 before the one the adjoint pairs with (the snapshot taken
+                                 before the update, src/serialcalls.cu:60), scale dt */
+#define FWI_MODE_EXACT 1      /* the exact discrete adjoint of the forward step including the
+                                 CPML memory variables: dJ/dv_hor, dJ/dv_po, dJ/dv_nmo of
+                                 J = 1/2 sum mask (d - d_obs)^2 */
+
+#define FWI_PREC_FP32 0
+#define FWI_PREC_FP64 1
+
+/* How the forward images that the imaging condition needs are kept. */
+#define FWI_STORE_FULL 0       /* every step, in HBM */
+#define FWI_STORE_CHECKPOINT 1 /* full states every ckpt_every steps; segments recomputed */
+
+/* Element type of stored images (per-snapshot scaled for FP16). */
+#define FWI_SPREC_NATIVE 0 /* same as the compute precision */
+#define FWI_SPREC_FP16 1
+#define FWI_SPREC_BF16 2
+
+typedef struct {
+    int nx, nz;       /* grid points including the 4-point frame (src/main.c:39-40) */
+    float dh, dt;     /* grid step (m) and time step (s) */
+    int cpml;         /* absorbing layer width in points (src/main.c:38) */
+    float f_cpml;     /* frequency (Hz) in the CPML alpha term (src/parallelcalls.cu:25) */
+    float vmax;       /* CPML velocity, 6000 in the reference (src/main.c:51) */
+    float r_coef;     /* CPML reflection coefficient, 1e-6 (src/main.c:48) */
+    int nt_max;       /* longest shot (time steps) */
+    int max_shots;    /* shots resident on the device at once */
+    int max_window;   /* widest shot aperture in columns (0 = nx) */
+    int max_receivers;/* most receivers of one shot (0 = max_window) */
+    int mode;         /* FWI_MODE_* */
+    int precision;    /* FWI_PREC_* */
+    int store;        /* FWI_STORE_* */
+    int store_prec;   /* FWI_SPREC_* */
+    int ckpt_every;   /* checkpoint interval for FWI_STORE_CHECKPOINT (0 = automatic) */
+    int device;       /* CUDA device ordinal */
+} fwi_config;
+
+/* One shot.  Coordinates are 0-based model grid points.  The simulation grid
+ * of the shot is the model's columns [x0, x0 + nxw) (all rows) with its own
+ * frame and CPML layers at the window edges; nxw = 0 means the whole model.
+ * The source (sx, sz) and the receivers (row rz, columns [rx0, rx1)) must lie
+ * inside the window's updated interior.  The reference's geometry is
+ * sx = posShots[i] - 1, sz = rz = 4 (sz - 1 with sz = 5), rx = [CPML, nx - CPML)
+ * (src/main.c:45-46, 260-262; src/parallelcalls.cu:107-116). */
+typedef struct {
+    int sx, sz;
+    int rz, rx0, rx1;
+    int nt;
+    int x0, nxw;
+} fwi_shot;
+
+/* Defaults: the reference's constants (src/main.c:38-52) on a 201 x 201 grid. */
+void fwi_config_default(fwi_config *cfg);
+
+/* Device bytes a context with this configuration allocates. */
+size_t fwi_config_bytes(const fwi_config *cfg);
+
+int fwi_create(const fwi_config *cfg, void **ctx_out);
+void fwi_destroy(void *ctx);
+const char *fwi_strerror(int status);
+/* The cudaError_t behind the last FWI_ERR_CUDA of this context (0 if none). */
+int fwi_last_cuda_error(void *ctx);
+
+/* Models as squared velocities [nz][nx].  Replaces src/serialcalls.cu:17-21 when given
+ * (Vp, epsilon, delta) through fwi_set_model_vti. */
+int fwi_set_model(void *ctx, const void *v_hor, const void *v_po, const void *v_nmo);
+int fwi_set_model_vti(void *ctx, const void *vp, const void *eps, const void *delta);
+int fwi_get_model(void *ctx, void *v_hor, void *v_po, void *v_nmo);
+
+/* Source wavelet shared by all shots, nt samples (src/main.c:328-333 makes a Ricker). */
+int fwi_set_wavelet(void *ctx, const void *wavelet, int nt);
+/* Ricker wavelet of src/main.c:328-332 with peak frequency f. */
+int fwi_set_ricker(void *ctx, float f, int nt);
+
+/* Forward modelling (src/main.c:334-366).  traces: per shot, [nt][rx1 - rx0], shots
+ * concatenated in order. */
+int fwi_forward(void *ctx, const fwi_shot *shots, int nshots, void *traces);
+
+/* Misfit J = 1/2 sum mask (d - obs)^2 (FP64) and, with gradients requested,
+ * dJ/dv_hor, dJ/dv_po, dJ/dv_nmo summed over the shots, [nz][nx] each
+ * (src/main.c:408-534 with the MPI reduction replaced by an on-device sum).
+ * obs: per shot [nt][nrec], concatenated.  mask: per shot [nrec] bytes
+ * (0 = dropped trace), concatenated, or NULL.  g_* may be NULL (the gradient
+ * then stays in the context for the L-BFGS calls below). */
+int fwi_gradient(void *ctx, const fwi_shot *shots, int nshots, const void *obs,
+                 const unsigned char *mask, void *g_vh, void *g_vp, void *g_vn, double *misfit);
+
+/* Misfit only (forward + residual), e.g. for line-search trials (src/main.c:695-737). */
+int fwi_misfit(void *ctx, const fwi_shot *shots, int nshots, const void *obs,
+               const unsigned char *mask, double *misfit);
+
+/* Replaces the context's gradient, e.g. with one summed over several processes
+ * (the role of src/main.c:510-538's MPI reduction), before the update calls below. */
+int fwi_set_gradient(void *ctx, const void *g_vh, const void *g_vp, const void *g_vn);
+
+/* ---- model update: steepest descent and L-BFGS, on the device ----
+ * Pairings as src/main.c:573: (v_po, dJ/dv_po), (v_nmo, dJ/dv_nmo), (v_hor, dJ/dv_hor),
+ * each with its own scalars.  Dot products accumulate in FP64. */
+
+/* First iteration (src/main.c:539-568): normalise each gradient by its L2 norm below
+ * the near-surface layer and step the model by (a_hor, a_po, a_nmo).  Keeps the model
+ * and gradient as the pair the next direction differences against. */
+int fwi_first_step(void *ctx, float a_hor, float a_po, float a_nmo);
+
+/* L-BFGS two-loop direction (src/main.c:569-682, memory m <= 16) from the last gradient.
+ * stats (optional, 12 doubles, order v_hor, v_po, v_nmo): gamma[3], 1/(y.s)[3], y.s[3], y.y[3]
+ * of the newest pair. */
+int fwi_lbfgs_direction(void *ctx, int m, double *stats);
+
+/* Trial model m = m_back - alpha r below the layer, optional clamps, v_hor >= v_nmo
+ * (src/parallelcalls.cu:343-404). */
+int fwi_lbfgs_update(void *ctx, float alpha_v, float alpha_d, float alpha_e, int flag_min,
+                     int flag_max);
+
+/* Model back to m_back (src/main.c:777-784). */
+int fwi_restore_model(void *ctx);
+
+/* Chain rule to the Vp / epsilon / delta parameterisation of the current model:
+ * dJ/dVp = 2 Vp (g_po + (1 + 2 eps) g_hor + (1 + 2 delta) g_nmo),
+ * dJ/deps = 2 Vp^2 g_hor, dJ/ddelta = 2 Vp^2 g_nmo (outputs [nz][nx]). */
+int fwi_gradient_vti(void *ctx, void *g_vp, void *g_eps, void *g_delta);
+
+/* Timing of the last fwi_gradient / fwi_misfit / fwi_forward call (device time, ms):
+ * out[0] total, out[1] forward, out[2] adjoint, out[3] other. */
+int fwi_last_timing(void *ctx, float *out4);
+
+/* How many of this library's kernels the last call launched. */
+long fwi_last_launches(void *ctx);
+
+/* Host-side helper, no GPU needed: the CPML strip points of an nx x nz grid
+ * (the points src/parallelcalls.cu:55 updates), in the order the strip kernels
+ * visit them.  Returns the count; writes at most cap pairs. */
+long fwi_strip_points(int nx, int nz, int cpml, int *ix, int *iz, long cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
