@@ -1,0 +1,394 @@
+"""Benchmark: gradient shots/s of the batched native path on the C2 workload.
+
+One step = one gradient evaluation of the whole batch (32 shots of the
+601 x 301, nt = 3000 C2 workload): forward with image storage, residual and
+FP64 misfit, adjoint + imaging, on-device shot reduction.  Inputs (observed
+data) and outputs (gradients) are resident in HBM for `value`; `e2e` passes
+pinned host buffers through the public C-ABI (fwi_gradient), so the
+host-to-device copy of the observed data and the device-to-host copy of the
+gradients and misfit are inside its timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+Multi-GPU (torchrun): every rank runs its own C2 batch on its own GPU (weak
+scaling, no collective on the data path); rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "gradient shots/s & Gpt-updates/s, batched+ckpt vs plain GPU, grad rel-err≤1e-4"
+ALG_BYTES_FWD = 36   # B per point update: P,F now and previous, P,F next, three models
+ALG_BYTES_ADJ = 68   # adjoint 36 + forward image 8 + three gradient read-modify-writes 24
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile(name):
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_launch:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.p = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self, gpu_index=0):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in open(self.path):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9 or f[0] != str(gpu_index):
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        load = [s for s in sm if mx and s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    n = int(os.environ.get("WORLD_SIZE", "1"))
+    if n <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, n, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------- CPU (oracle) timing
+
+def cpu_sample(w, seconds=15.0, threads=None):
+    """Time the oracle's reference-arithmetic gradient (src/main.c:408-495 sequence) of one
+    shot over a bounded number of steps; returns (shots/s extrapolated, threads, sample)."""
+    from oracle import pyoracle as po
+    po.build()
+    threads = threads or os.cpu_count() or 1
+    po.set_threads(threads)
+    vh, vp, vn = w.squared(initial=True)
+    s = w.shots[0]
+    probe_nt = 40
+    ax, bx, az, bz = po.cpml_profiles(w.nx, w.nz, w.cpml, w.dh, w.dt, w.f)
+    def run(nt):
+        p = dict(nx=w.nx, nz=w.nz, nt=nt, cpml=w.cpml, dh=w.dh, dt=w.dt, ax=ax, bx=bx, az=az, bz=bz,
+                 source=po.ricker(nt, w.dt, w.f), vh=vh, vp=vp, vn=vn)
+        obs = np.zeros((nt, w.nx), np.float32)
+        t0 = time.perf_counter()
+        po.gradient_shot(p, s["sx"] + 1, s["sz"] + 1, obs)
+        return time.perf_counter() - t0
+    t_probe = run(probe_nt)
+    nt = int(max(probe_nt, min(s["nt"], probe_nt * seconds / max(t_probe, 1e-3))))
+    t = run(nt)
+    per_step = t / nt
+    shots_per_s = 1.0 / (per_step * s["nt"])
+    return shots_per_s, threads, (f"one {w.nx}x{w.nz} shot, {nt} forward + {nt} adjoint steps of "
+                                  f"{s['nt']}, extrapolated to the full shot; {t:.1f} s")
+
+
+# ----------------------------------------------------------------- GPU timing
+
+def native_arm(args, rank, world, dist):
+    import torch
+
+    import fwi_gb300
+    from fwi_gb300 import synth
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    w = synth.WORKLOADS[args.workload](shots=args.shots, nt=args.nt) if args.workload in ("C2", "C3") \
+        else synth.WORKLOADS[args.workload]()
+    shots = fwi_gb300.make_shots(w.shots)
+    mode = fwi_gb300.MODE_EXACT if args.mode == "exact" else fwi_gb300.MODE_REF_COMPAT
+    sprec = {"fp32": fwi_gb300.SPREC_NATIVE, "fp16": fwi_gb300.SPREC_FP16, "bf16": fwi_gb300.SPREC_BF16}[args.store]
+    nrec = max(s["rx1"] - s["rx0"] for s in w.shots)
+
+    def context(max_shots, precision=fwi_gb300.PREC_FP32, store_prec=sprec):
+        c = fwi_gb300.Context(nx=w.nx, nz=w.nz, dh=w.dh, dt=w.dt, cpml=w.cpml, f_cpml=w.f, nt_max=w.nt,
+                              max_shots=max_shots, max_receivers=nrec, mode=mode, precision=precision,
+                              store_prec=store_prec, device=dev)
+        c.set_ricker(w.f, w.nt)
+        return c
+
+    # observed data from the true model, then the initial model
+    ctx = context(min(args.batch, len(w.shots)))
+    ctx.set_model(*w.squared())
+    ntr = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots)
+    obs_d = torch.zeros(ntr, dtype=torch.float32, device="cuda")
+    ctx.forward(shots, out=obs_d)
+    ctx.set_model(*w.squared(initial=True))
+    g_d = [torch.zeros((w.nz, w.nx), dtype=torch.float32, device="cuda") for _ in range(3)]
+
+    def step():
+        J, *_ = ctx.gradient(shots, obs_d, w.mask, out=g_d)
+        return J
+
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks()
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    t_fwd = t_adj = t_tot = 0.0
+    e0.record()
+    for _ in range(args.steps):
+        J = step()
+        t = ctx.last_timing()
+        t_tot += float(t[0])
+        t_fwd += float(t[1])
+        t_adj += float(t[2])
+        launches += ctx.last_launches()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(dist)
+    clk = clocks.stop(dev)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(dist, ms)
+    nshots = len(w.shots)
+    upd = w.point_updates()
+    value = world * nshots / (ms / 1e3)
+
+    # end to end: pinned host observed data in, host gradients and misfit out
+    obs_h = obs_d.cpu().pin_memory()
+    g_h = [torch.zeros((w.nz, w.nx), dtype=torch.float32).pin_memory() for _ in range(3)]
+    for _ in range(2):
+        ctx.gradient(shots, obs_h, w.mask, out=g_h)
+    barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.gradient(shots, obs_h, w.mask, out=g_h)
+    torch.cuda.synchronize()
+    ms_e2e = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps)
+    barrier(dist)
+
+    out = None
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        # dominant kernel: the adjoint step (strip pass + main pass), timed on its stream
+        pts = sum((s["nxw"] or w.nx) * w.nz * s["nt"] for s in w.w_shots) if hasattr(w, "w_shots") else \
+            sum((s["nxw"] or w.nx) * w.nz * s["nt"] for s in w.shots)
+        adj_gbs = ALG_BYTES_ADJ * pts / (t_adj / args.steps / 1e3) / 1e9
+        fwd_gbs = ALG_BYTES_FWD * pts / (t_fwd / args.steps / 1e3) / 1e9
+        traffic = traffic_from_profile(f"k_adj_main_{args.workload}_traffic.txt")
+        launches_per_step = 2 * w.nt
+        out = {
+            "metric": METRIC, "value": round(value, 4), "unit": "shots/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded C2 model, observed data modelled on the GPU from the true model)",
+            "config": {"workload": w.name, "nx": w.nx, "nz": w.nz, "dh": w.dh, "dt": w.dt, "nt": w.nt,
+                       "shots": nshots, "receivers_per_shot": nrec, "ricker_hz": w.f, "cpml": w.cpml,
+                       "mode": args.mode, "image_store": f"full, {args.store}", "batch": args.batch,
+                       "l2": "inputs larger than L2 (observed data 231 MB, images streamed through HBM)"},
+            "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
+            "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
+                    "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
+            "roofline": {"bound": "hbm", "kernel": "adjoint step (k_adj_strip + k_adj_main)",
+                         "achieved": round(adj_gbs, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(adj_gbs / hbm, 4), "peak_kind": peak_kind,
+                         "traffic": traffic, "forward_step_achieved": round(fwd_gbs, 1),
+                         "forward_frac": round(fwd_gbs / hbm, 4),
+                         "gradient_frac": round((ALG_BYTES_FWD + ALG_BYTES_ADJ) * pts / (t_tot / args.steps / 1e3)
+                                                / 1e9 / hbm, 4)},
+            "gpu_launches": int(launches),
+            "phase_ms": {"forward": round(t_fwd / args.steps, 3), "adjoint": round(t_adj / args.steps, 3),
+                         "other": round((t_tot - t_fwd - t_adj) / args.steps, 3)},
+            "misfit": J,
+        }
+        if clk:
+            out["clocks"] = clk
+    del ctx
+
+    if rank == 0 and not args.skip_extras:
+        # plain per-shot FP32 path (one shot per launch sequence, FP32 images), on a subset
+        sub = fwi_gb300.make_shots(w.shots[: args.plain_shots])
+        nsub = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots[: args.plain_shots])
+        c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE)
+        c1.set_model(*w.squared(initial=True))
+        c1.gradient(sub, obs_d[:nsub])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c1.gradient(sub, obs_d[:nsub])
+        torch.cuda.synchronize()
+        plain = args.plain_shots / (time.perf_counter() - t0)
+        ref32 = c1.gradient(sub, obs_d[:nsub].cpu().numpy())
+        del c1
+        out["plain_gpu"] = {"value": round(plain, 4), "unit": "shots/s",
+                            "how": f"max_shots=1, FP32 images, {args.plain_shots} shots timed",
+                            "speedup": round(value / world / plain, 2)}
+        # gradient error of this configuration against the FP64 GPU path, same shots
+        c64 = context(args.plain_shots, precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE)
+        c64.set_model(*(a.astype(np.float64) for a in w.squared(initial=True)))
+        r64 = c64.gradient(sub, obs_d[:nsub].cpu().numpy().astype(np.float64))
+        del c64
+        cx = context(args.plain_shots)
+        cx.set_model(*w.squared(initial=True))
+        rx = cx.gradient(sub, obs_d[:nsub].cpu().numpy())
+        del cx
+        rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        out["grad_rel_err_vs_fp64"] = {
+            "this_config": [round(rel(a, b), 7) for a, b in zip(rx[1:], r64[1:])],
+            "fp32_images": [round(rel(a, b), 7) for a, b in zip(ref32[1:], r64[1:])],
+            "order": "v_hor, v_po, v_nmo", "shots": args.plain_shots,
+            "misfit_rel_err": abs(rx[0] - r64[0]) / abs(r64[0])}
+        # L-BFGS two-loop (m = 5) on this grid, FP64 dots
+        from fwi_gb300 import Context
+        cl = context(1)
+        cl.set_model(*w.squared(initial=True))
+        cl.set_gradient(*(a.astype(np.float32) for a in r64[1:]))
+        cl.first_step(3e5, 2e5, 2.5e5)
+        rng = np.random.default_rng(0)
+        for it in range(6):
+            cl.set_gradient(*(a.astype(np.float32) * (1 + 0.01 * it) + rng.standard_normal(a.shape).astype(np.float32)
+                              * 1e-3 * float(np.abs(a).max()) for a in r64[1:]))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            cl.lbfgs_direction(5)
+            tl = time.perf_counter() - t0
+            cl.lbfgs_update(1e-3, 1e-3, 1e-3)
+        out["lbfgs_direction_ms"] = round(tl * 1e3, 3)
+        del cl
+    if rank == 0 and not args.skip_cpu:
+        v, thr, sample = cpu_sample(w, seconds=args.cpu_seconds)
+        out["cpu_baseline"] = {"value": round(v, 6), "unit": "shots/s", "cores": thr, "kind": "port",
+                               "sample": sample}
+    return out
+
+
+def reference_arm(args, rank, world, dist):
+    """The reference's CPU arithmetic (oracle restatement; the reference has no CPU
+    path of its own), all host threads, bounded samples of the same workload."""
+    if rank != 0:
+        return None
+    from fwi_gb300 import synth
+    w = synth.WORKLOADS[args.workload](shots=args.shots, nt=args.nt) if args.workload in ("C2", "C3") \
+        else synth.WORKLOADS[args.workload]()
+    secs = max(2.0, args.cpu_seconds / max(1, args.steps))
+    vals = []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_sample(w, seconds=1.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, thr, sample = cpu_sample(w, seconds=secs)
+        vals.append(v)
+    dt = time.perf_counter() - t0
+    v = statistics.median(vals)
+    return {"metric": METRIC, "value": round(v, 6), "unit": "shots/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "impl": "reference",
+            "data": "synthetic", "config": {"workload": w.name, "nx": w.nx, "nz": w.nz, "nt": w.nt,
+                                            "shots": len(w.shots)},
+            "cpu_baseline": {"value": round(v, 6), "unit": "shots/s", "cores": thr, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(v, 6), "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--workload", default="C2")
+    ap.add_argument("--shots", type=int, default=32)
+    ap.add_argument("--nt", type=int, default=3000)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--mode", default="exact", choices=["exact", "ref"])
+    ap.add_argument("--store", default="fp16", choices=["fp32", "fp16", "bf16"])
+    ap.add_argument("--plain-shots", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-extras", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, dist = dist_setup()
+    if args.impl == "reference":
+        out = reference_arm(args, rank, world, dist)
+    else:
+        out = native_arm(args, rank, world, dist)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

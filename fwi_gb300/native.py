@@ -171,6 +171,24 @@ def strip_points(nx, nz, cpml):
     return ix[:n], iz[:n]
 
 
+def _checked(x, dtype, size, what):
+    """Host numpy arrays must have the context's element type and at least `size` elements."""
+    if isinstance(x, np.ndarray):
+        if x.dtype != dtype:
+            raise TypeError(f"{what}: dtype {x.dtype}, the context computes in {np.dtype(dtype)}")
+        if x.size < size:
+            raise ValueError(f"{what}: {x.size} elements, {size} needed")
+        if not x.flags.c_contiguous:
+            raise ValueError(f"{what}: not C-contiguous")
+    elif hasattr(x, "dtype") and hasattr(x, "numel"):
+        want = "torch.float64" if np.dtype(dtype) == np.float64 else "torch.float32"
+        if str(x.dtype) != want and what != "mask":
+            raise TypeError(f"{what}: dtype {x.dtype}, expected {want}")
+        if x.numel() < size:
+            raise ValueError(f"{what}: {x.numel()} elements, {size} needed")
+    return x
+
+
 class Context:
     """One native context (include/fwi.h)."""
 
@@ -209,10 +227,16 @@ class Context:
     def handle(self):
         return self._h
 
+    def _grid(self, *arrays, what="model"):
+        n = self.cfg.nx * self.cfg.nz
+        return [_checked(a, self.dtype, n, what) for a in arrays]
+
     def set_model(self, vh, vp, vn):
+        vh, vp, vn = self._grid(vh, vp, vn)
         _check(lib().fwi_set_model(self._h, ptr(vh), ptr(vp), ptr(vn)), "fwi_set_model")
 
     def set_model_vti(self, vel, eps, delta):
+        vel, eps, delta = self._grid(vel, eps, delta)
         _check(lib().fwi_set_model_vti(self._h, ptr(vel), ptr(eps), ptr(delta)), "fwi_set_model_vti")
 
     def get_model(self):
@@ -222,6 +246,7 @@ class Context:
 
     def set_wavelet(self, w):
         w = np.ascontiguousarray(w, self.dtype) if isinstance(w, np.ndarray) else w
+        _checked(w, self.dtype, len(w), "wavelet")
         _check(lib().fwi_set_wavelet(self._h, ptr(w), len(w)), "fwi_set_wavelet")
 
     def set_ricker(self, f, nt):
@@ -231,6 +256,7 @@ class Context:
         n = sum(s.nt * s.nrec for s in shots)
         if out is None:
             out = np.zeros(n, self.dtype)
+        _checked(out, self.dtype, n, "traces")
         _check(lib().fwi_forward(self._h, shots, len(shots), ptr(out)), "fwi_forward")
         return out
 
@@ -238,18 +264,27 @@ class Context:
         """Returns (misfit, g_vh, g_vp, g_vn); `out` may give three destination arrays."""
         if out is None:
             out = [np.zeros((self.cfg.nz, self.cfg.nx), self.dtype) for _ in range(3)]
+        self._grid(*out, what="gradient")
+        self._inputs(shots, obs, mask)
         J = C.c_double(0)
         _check(lib().fwi_gradient(self._h, shots, len(shots), ptr(obs), ptr(mask),
                                   *[ptr(o) for o in out], C.byref(J)), "fwi_gradient")
         return (J.value, *out)
 
+    def _inputs(self, shots, obs, mask):
+        _checked(obs, self.dtype, sum(s.nt * s.nrec for s in shots), "obs")
+        if mask is not None:
+            _checked(mask, np.uint8, sum(s.nrec for s in shots), "mask")
+
     def misfit(self, shots, obs, mask=None):
+        self._inputs(shots, obs, mask)
         J = C.c_double(0)
         _check(lib().fwi_misfit(self._h, shots, len(shots), ptr(obs), ptr(mask), C.byref(J)),
                "fwi_misfit")
         return J.value
 
     def set_gradient(self, gh, gp, gn):
+        gh, gp, gn = self._grid(gh, gp, gn, what="gradient")
         _check(lib().fwi_set_gradient(self._h, ptr(gh), ptr(gp), ptr(gn)), "fwi_set_gradient")
 
     def first_step(self, a_hor, a_po, a_nmo):

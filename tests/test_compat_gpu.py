@@ -160,16 +160,16 @@ def test_update_lbfgs_bitexact(L):
 
 
 def _random_state(seed):
+    """White-noise fields (zero frame): no cancellation inside the stencils, so an
+    FP32 evaluation stays within a few ulp of the reference's FP64 one."""
     rng = np.random.default_rng(seed)
 
-    def smooth():
+    def field():
         a = rng.standard_normal((NZ, NX))
-        for _ in range(3):
-            a = (a + np.roll(a, 1, 0) + np.roll(a, -1, 0) + np.roll(a, 1, 1) + np.roll(a, -1, 1)) / 5
         a[:4] = a[-4:] = 0
         a[:, :4] = a[:, -4:] = 0
         return a.astype(np.float32)
-    return smooth
+    return field
 
 
 def test_single_step_kernels_against_oracle(L):
