@@ -34,14 +34,16 @@ __host__ __device__ inline bool in_strip(int ix, int iz, int nx, int nz, int cpm
     return interior(ix, iz, nx, nz) && (ix < cpml || ix > nx - cpml - 1 || iz > nz - cpml - 1);
 }
 
-// Sum of two neighbours at distance k (second derivative taps) from a strided
-// array; `s` is 1 for x and the row pitch for z.
+// Second derivative (unnormalised) of a strided array, `s` = 1 for x and the
+// row pitch for z, on differences from the centre value (the weights sum to
+// zero; see d2x_tile).
 template <typename T>
 __device__ __forceinline__ T d2_strided(const T *__restrict__ f, long i, long s)
 {
     using C = Coef<T>;
-    return C::d2_0 * f[i] + C::d2_1 * (f[i + s] + f[i - s]) - C::d2_2 * (f[i + 2 * s] + f[i - 2 * s]) +
-           C::d2_3 * (f[i + 3 * s] + f[i - 3 * s]) - C::d2_4 * (f[i + 4 * s] + f[i - 4 * s]);
+    const T o = f[i];
+    return C::d2_1 * ((f[i + s] - o) + (f[i - s] - o)) - C::d2_2 * ((f[i + 2 * s] - o) + (f[i - 2 * s] - o)) +
+           C::d2_3 * ((f[i + 3 * s] - o) + (f[i - 3 * s] - o)) - C::d2_4 * ((f[i + 4 * s] - o) + (f[i - 4 * s] - o));
 }
 
 template <typename T>

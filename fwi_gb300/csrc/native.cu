@@ -356,6 +356,16 @@ __global__ void k_grad_vti(const T *vh, const T *vp, const T *vn, const T *gh, c
     }
 }
 
+// Steps between checkpoints: minimises checkpoint (8 full arrays each) plus
+// segment image memory (2 arrays of the image type per step) for nt steps.
+int checkpoint_interval(const fwi_config &c)
+{
+    if (c.ckpt_every > 0) return std::min(c.ckpt_every, c.nt_max);
+    const double img = c.store_prec == FWI_SPREC_NATIVE ? 1.0 : 0.5 * (c.precision == FWI_PREC_FP64 ? 0.5 : 1.0);
+    int k = (int)std::ceil(std::sqrt(8.0 * c.nt_max / (2.0 * img)));
+    return std::max(1, std::min(k, c.nt_max));
+}
+
 inline unsigned elt_grid(long n)
 {
     long b = (n + 255) / 256;
@@ -411,8 +421,12 @@ template <typename T> struct Ctx : CtxBase {
     bool have_model = false, have_wavelet = false, models_dirty = true;
     int wavelet_nt = 0;
     // batch
-    T *lvl[4] = {}, *cp[8] = {}, *gs[3] = {};
+    T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {};
     void *store = nullptr;
+    // checkpointing: full states every ck_every steps, segment recompute buffers
+    int ck_every = 0, n_ck = 0;
+    T *ck = nullptr;                 // [n_ck][8][B * slot]: P, F, their increments, CPML x4
+    T *rlvl[6] = {}, *rcp[4] = {};
     float *scale = nullptr, *amax = nullptr;
     T *rec = nullptr, *obs = nullptr;
     unsigned char *mask = nullptr;
@@ -480,6 +494,14 @@ template <typename T> struct Ctx : CtxBase {
         for (auto &p : lvl) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : cp) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : gs) TRY(alloc(&p, (size_t)B * slot));
+        if (cfg.store == FWI_STORE_CHECKPOINT) {
+            ck_every = checkpoint_interval(cfg);
+            n_ck = (nt_max + ck_every - 1) / ck_every;
+            n_img = ck_every;
+            TRY(alloc(&ck, (size_t)n_ck * 8 * B * slot));
+            for (auto &p : rlvl) TRY(alloc(&p, (size_t)B * slot));
+            for (auto &p : rcp) TRY(alloc(&p, (size_t)B * slot));
+        }
         {
             void *q0 = nullptr;
             TRY(cudaMalloc(&q0, (size_t)B * n_img * 2 * slot * store_elem()));
@@ -621,7 +643,7 @@ template <typename T> struct Ctx : CtxBase {
         Batch<T> b;
         b.B = nb; b.nz = nz; b.pitch = pitch; b.mpitch = mpitch; b.cpml = cfg.cpml; b.nt_max = nt_max;
         b.slot = slot;
-        for (int k = 0; k < 4; k++) b.lvl[k] = lvl[k];
+        for (int k = 0; k < 6; k++) b.lvl[k] = lvl[k];
         for (int k = 0; k < 8; k++) b.cp[k] = cp[k];
         for (int k = 0; k < 3; k++) b.g[k] = gs[k];
         b.store = store; b.store_type = store_type(); b.n_img = n_img;
@@ -632,6 +654,24 @@ template <typename T> struct Ctx : CtxBase {
         b.img_scale = cfg.mode == FWI_MODE_EXACT ? (T)cfg.dt * (T)cfg.dt : (T)cfg.dt;
         b.status = status;
         return b;
+    }
+
+    int save_checkpoint(int k, int nb, int cur)
+    {
+        const size_t bytes = (size_t)nb * slot * sizeof(T);
+        T *src[8] = {lvl[cur], lvl[2 + cur], lvl[4], lvl[5], cp[0], cp[1], cp[2], cp[3]};
+        for (int a = 0; a < 8; a++)
+            TRY(cudaMemcpyAsync(ck + ((size_t)k * 8 + a) * B * slot, src[a], bytes, cudaMemcpyDeviceToDevice, st));
+        return FWI_OK;
+    }
+
+    int restore_checkpoint(int k, int nb, int cur)
+    {
+        const size_t bytes = (size_t)nb * slot * sizeof(T);
+        T *dst[8] = {rlvl[cur], rlvl[2 + cur], rlvl[4], rlvl[5], rcp[0], rcp[1], rcp[2], rcp[3]};
+        for (int a = 0; a < 8; a++)
+            TRY(cudaMemcpyAsync(dst[a], ck + ((size_t)k * 8 + a) * B * slot, bytes, cudaMemcpyDeviceToDevice, st));
+        return FWI_OK;
     }
 
     // Forward (+ residual + adjoint) of all shots, batch by batch.
@@ -684,9 +724,14 @@ template <typename T> struct Ctx : CtxBase {
             Batch<T> b = batch_view(nb);
             cudaEvent_t e0 = ev[1], e1 = ev[2], e2 = ev[3];
             TRY(cudaEventRecord(e0, st));
+            const bool ckpt = want_grad && cfg.store == FWI_STORE_CHECKPOINT;
             int cur = 0;
             for (int g = 0; g < ntb; g++) {
-                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, want_grad ? g : -1, exact, st);
+                if (ckpt && g % ck_every == 0) {
+                    int rc2 = save_checkpoint(g / ck_every, nb, cur);
+                    if (rc2) return rc2;
+                }
+                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt) ? g : -1, exact, st);
                 cur ^= 1;
             }
             TRY_LAUNCH();
@@ -707,13 +752,49 @@ template <typename T> struct Ctx : CtxBase {
                 for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
                 cur = 0;
                 int zsel = 0;
-                for (int j = 0; j < ntb; j++) {
-                    fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, st);
-                    cur ^= 1;
-                    zsel ^= 1;
+                if (!ckpt) {
+                    for (int j = 0; j < ntb; j++) {
+                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, st);
+                        cur ^= 1;
+                        zsel ^= 1;
+                    }
+                    TRY_LAUNCH();
+                    launches += 2L * ntb;
+                } else {
+                    // segments from the last: recompute its images from the checkpoint, then
+                    // run the adjoint iterations that image inside it
+                    const int lag = exact ? 0 : 1;
+                    Batch<T> rb = b;
+                    // frames of the recompute levels stay zero: never written by the steps
+                    for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+                    for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
+                    for (int k = 0; k < 4; k++) rb.cp[k] = rcp[k];
+                    int j = 0;
+                    for (int seg = (ntb - 1) / ck_every; seg >= 0; seg--) {
+                        const int a = seg * ck_every, e = std::min(a + ck_every, ntb);
+                        int rcur = a & 1;
+                        int rc2 = restore_checkpoint(seg, nb, rcur);
+                        if (rc2) return rc2;
+                        for (int g = a; g < e; g++) {
+                            fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, g - a, exact, st);
+                            rcur ^= 1;
+                        }
+                        launches += 2L * (e - a);
+                        for (; j < ntb && ntb - 1 - lag - j >= a; j++) {
+                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a, st);
+                            cur ^= 1;
+                            zsel ^= 1;
+                            launches += 2;
+                        }
+                    }
+                    for (; j < ntb; j++) {  // iterations without an image (reference lag)
+                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, st);
+                        cur ^= 1;
+                        zsel ^= 1;
+                        launches += 2;
+                    }
+                    TRY_LAUNCH();
                 }
-                TRY_LAUNCH();
-                launches += 2L * ntb;
                 k_accumulate_gradient<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(
                     grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, nb, nx, nz, mpitch, pitch, slot);
                 TRY_LAUNCH();
@@ -959,8 +1040,14 @@ size_t fwi_config_bytes(const fwi_config *c)
     const long nrec = c->max_receivers > 0 ? c->max_receivers : win;
     size_t b = 0;
     b += (size_t)(6 + 3 + 12) * mslot * e;                 // models, gradient, L-BFGS work arrays
-    b += (size_t)c->max_shots * slot * e * (4 + 8 + 3);    // levels, CPML state, per-shot gradients
-    b += (size_t)c->max_shots * c->nt_max * 2 * slot * se; // images
+    b += (size_t)c->max_shots * slot * e * (6 + 8 + 3);    // levels, CPML state, per-shot gradients
+    if (c->store == FWI_STORE_CHECKPOINT) {
+        const long k = checkpoint_interval(*c), n = (c->nt_max + k - 1) / k;
+        b += (size_t)c->max_shots * slot * e * (8 * n + 10); // checkpoints, recompute state
+        b += (size_t)c->max_shots * k * 2 * slot * se;       // images of one segment
+    } else {
+        b += (size_t)c->max_shots * c->nt_max * 2 * slot * se; // images
+    }
     b += (size_t)c->max_shots * c->nt_max * nrec * e * 2;  // records and observed data
     return b;
 }
@@ -973,7 +1060,9 @@ int fwi_create(const fwi_config *cfg, void **out)
         cfg->max_shots <= 0 || !(cfg->dh > 0) || !(cfg->dt > 0) || cfg->max_window < 0 || cfg->max_window > cfg->nx)
         return FWI_ERR_ARG;
     if (cfg->mode != FWI_MODE_EXACT && cfg->mode != FWI_MODE_REF_COMPAT) return FWI_ERR_ARG;
-    if (cfg->store != FWI_STORE_FULL) return FWI_ERR_UNSUPPORTED;
+    if (cfg->store != FWI_STORE_FULL && cfg->store != FWI_STORE_CHECKPOINT) return FWI_ERR_ARG;
+    if (cfg->store_prec < FWI_SPREC_NATIVE || cfg->store_prec > FWI_SPREC_BF16) return FWI_ERR_ARG;
+    if (cfg->precision == FWI_PREC_FP64 && cfg->store_prec != FWI_SPREC_NATIVE) return FWI_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device) {
         cudaGetLastError();

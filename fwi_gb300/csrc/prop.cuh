@@ -138,6 +138,7 @@ k_fwd_main(Batch<T> b, int g, int ntb, int cur, int img_slot)
     const long so = (long)s * b.slot;
     const T *P = b.lvl[cur] + so, *F = b.lvl[2 + cur] + so;
     T *Pn = b.lvl[1 - cur] + so, *Fn = b.lvl[3 - cur] + so;
+    T *Pv = b.lvl[4] + so, *Fv = b.lvl[5] + so;
 
     __shared__ T sP[PTZ][PXW];
     __shared__ T sF[PZH][PTX];
@@ -182,9 +183,13 @@ k_fwd_main(Batch<T> b, int g, int ntb, int cur, int img_slot)
             }
             const long mi = (long)iz * b.mpitch + sh.x0 + ix;
             const T mpH = b.mp[mi] * H;
-            T pn = T(2) * sP[r][c + kRad] - Pn[i] + b.mh[mi] * G + mpH;
-            T fn = T(2) * sF[r + kRad][c] - Fn[i] + b.mn[mi] * G + mpH;
-            if (ix == sh.sx && iz == sh.sz) { pn += w; fn += w; }
+            T vp = Pv[i] + (b.mh[mi] * G + mpH);
+            T vf = Fv[i] + (b.mn[mi] * G + mpH);
+            if (ix == sh.sx && iz == sh.sz) { vp += w; vf += w; }
+            Pv[i] = vp;
+            Fv[i] = vf;
+            const T pn = sP[r][c + kRad] + vp;
+            const T fn = sF[r + kRad][c] + vf;
             Pn[i] = pn;
             Fn[i] = fn;
             if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1)
@@ -196,7 +201,9 @@ k_fwd_main(Batch<T> b, int g, int ntb, int cur, int img_slot)
             if (Cd::scaled) lmax = fmaxf(lmax, fmaxf(fabsf((float)pn), fabsf((float)fn)));
         }
     }
-    if (STORE && Cd::scaled) block_max_to(lmax, &b.amax[(long)s * (b.nt_max + 1) + g + 1]);
+    // the state's max bounds the next step's images (image_scale); recorded on every
+    // pass so that a segment recomputed from a checkpoint finds it
+    if (Cd::scaled) block_max_to(lmax, &b.amax[(long)s * (b.nt_max + 1) + g + 1]);
 }
 
 // ---------------------------------------------------------------- adjoint
@@ -347,6 +354,7 @@ k_adj_main(Batch<T> b, int j, int ntb, int cur, int zsel, int img_base)
     const long so = (long)s * b.slot;
     const T *lP = b.lvl[cur] + so, *lF = b.lvl[2 + cur] + so;
     T *lPn = b.lvl[1 - cur] + so, *lFn = b.lvl[3 - cur] + so;
+    T *lPw = b.lvl[4] + so, *lFw = b.lvl[5] + so;
     const int m = sh.nt - j;
 
     __shared__ T sU[PTZ][PXW];
@@ -454,13 +462,17 @@ k_adj_main(Batch<T> b, int j, int ntb, int cur, int zsel, int img_base)
             ex += (n1 + dxcx) + (n3 + dzdx);
             ez += (n2 + dxcz) + (n4 + dzcz);
         }
-        T pn = T(2) * lP[i] - lPn[i] + ex;
-        T fn = T(2) * lF[i] - lFn[i] + ez;
+        T wp = lPw[i] + ex;
+        T wf = lFw[i] + ez;
         if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1) {
             const T d = res_row[ix - sh.rx0];
-            pn += d;
-            fn += d;
+            wp += d;
+            wf += d;
         }
+        lPw[i] = wp;
+        lFw[i] = wf;
+        const T pn = lP[i] + wp;
+        const T fn = lF[i] + wf;
         lPn[i] = pn;
         lFn[i] = fn;
         if (img) {

@@ -23,7 +23,7 @@ enum StoreType { kStoreNative = 0, kStoreHalf = 1, kStoreBf16 = 2 };
 template <typename T> struct Batch {
     int B, nz, pitch, mpitch, cpml, nt_max;
     long slot;
-    T *lvl[4];      // P level 0, P level 1, F level 0, F level 1
+    T *lvl[6];      // P level 0, P level 1, F level 0, F level 1, P increment, F increment
     T *cp[8];       // CPML memory variables (forward uses 0..3)
     T *g[3];        // per-shot gradient accumulators: v_hor, v_po, v_nmo
     void *store;    // images: [B][n_img][2][slot] of the store type
@@ -46,8 +46,14 @@ template <typename T> struct Batch {
 // so every shot's adjoint starts at the same global iteration and the image
 // a given adjoint iteration needs sits at the same global step for all shots.
 
+// Time stepping is in increment form: u^{n+1} = u^n + v, v = v + dt^2 (...),
+// with u ping-ponged between two levels (neighbours of other blocks read the
+// old level) and the increment v updated in place.  Algebraically the
+// reference's leapfrog; in FP32 it keeps the low bits of each small update
+// that 2 u^n - u^{n-1} + dt^2 (...) rounds away.
+
 // Forward global step g.  `cur` is the level holding each shot's current
-// state; the new state overwrites level 1 - cur.  With img_slot >= 0 the
+// state; the new state goes to level 1 - cur.  With img_slot >= 0 the
 // step's images go to that slot (G, H for exact imaging, Dxx P and Dzz F for
 // the reference's).  Receiver traces are always recorded.
 template <typename T>
@@ -55,7 +61,7 @@ void launch_forward_step(const Batch<T> &b, int nx_max, int g, int ntb, int cur,
                          bool exact, cudaStream_t st);
 
 // Adjoint iteration j: lambda^m, m = nt_s - j, of every shot with nt_s > j.
-// `cur` holds lambda^{m+1}; lambda^m overwrites level 1 - cur.  `zsel`
+// `cur` holds lambda^{m+1}; lambda^m goes to level 1 - cur (increment form).  `zsel`
 // selects the ping-pong half of the exact adjoint's Z state.  The image of
 // global step ntb - 1 - lag - j (lag 0 exact, 1 reference) is read from slot
 // (that step - img_base); img_base <= that step is the caller's contract.

@@ -180,14 +180,16 @@ def main():
     for n in "q_gcz q_gdx q_gcx r_b1 r_b2 r_b3".split():
         out[f"lb0_{n}"] = st[n]
     out["lb0_sigma"], out["lb0_epsilon"], out["lb0_gamma"] = sig, eps, gam
+    # the model is backed up before the trial update (src/main.c:683-688), so the
+    # trial model is v_1 - alpha r
     vp2, vn2, vh2 = vp1.copy(), vn1.copy(), vh1.copy()
     ref.ref_update_lbfgs(P(st["r_b1"]), P(st["r_b2"]), P(st["r_b3"]), P(vp2), P(vn2), P(vh2),
-                         P(vp_i), P(vn_i), P(vh_i), nx, nz, 1.0, 1.0, 1.0, 1, 1, 1, 0, 0)
+                         P(vp1), P(vn1), P(vh1), nx, nz, 1.0, 1.0, 1.0, 1, 1, 1, 0, 0)
     out["vp_2"], out["vn_2"], out["vh_2"] = vp2, vn2, vh2
     # the same update with the optional clamps on (flags of src/parallelcalls.cu:343-404)
     vp3, vn3, vh3 = vp1.copy(), vn1.copy(), vh1.copy()
     ref.ref_update_lbfgs(P(st["r_b1"]), P(st["r_b2"]), P(st["r_b3"]), P(vp3), P(vn3), P(vh3),
-                         P(vp_i), P(vn_i), P(vh_i), nx, nz, 40.0, 40.0, 40.0, 1, 1, 1, 1, 1)
+                         P(vp1), P(vn1), P(vh1), nx, nz, 40.0, 40.0, 40.0, 1, 1, 1, 1, 1)
     out["vp_3"], out["vn_3"], out["vh_3"] = vp3, vn3, vh3
 
     # a deeper history: slots 0..1 filled with seeded curvature pairs, direction in slot 2

@@ -52,6 +52,17 @@ def P(t):
     return t.data_ptr()
 
 
+_KEEP = []
+
+
+def D(a):
+    """Device copy that stays alive for the whole test (a bare temporary would be
+    freed, and its memory handed to the next allocation, before the kernel runs)."""
+    t = dev(a)
+    _KEEP.append(t)
+    return t
+
+
 def rel_l2(a, b):
     return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
 
@@ -152,7 +163,7 @@ def test_update_lbfgs_bitexact(L):
     r = [dev(G[k]) for k in ("lb0_r_b1", "lb0_r_b2", "lb0_r_b3")]
     for alpha, fmin, fmax, tag in ((1.0, 0, 0, "2"), (40.0, 1, 1, "3")):
         vp, vn, vh = dev(G["vp_1"]), dev(G["vn_1"]), dev(G["vh_1"])
-        bp, bn, bh = dev(G["vp_i"]), dev(G["vn_i"]), dev(G["vh_i"])
+        bp, bn, bh = dev(G["vp_1"]), dev(G["vn_1"]), dev(G["vh_1"])
         L.update_LBFGS_h(P(r[0]), P(r[1]), P(r[2]), P(vp), P(vn), P(vh), P(bp), P(bn), P(bh), NX,
                          NZ, alpha, alpha, alpha, 1, 1, 1, fmin, fmax)
         assert np.array_equal(host(vp), G[f"vp_{tag}"]) and np.array_equal(host(vn), G[f"vn_{tag}"])
@@ -190,13 +201,13 @@ def test_single_step_kernels_against_oracle(L):
     p2o, r2o = np.zeros_like(Pp), np.zeros_like(Pp)
     O.orc_second_derivate_p_f32(ptr(Pp), ptr(Fp), ptr(p2o), ptr(r2o), dh2, NX, NZ)
     p2g, r2g = zeros(NZ, NX), zeros(NZ, NX)
-    L.SecondDerivate_P_h(P(dev(Pp)), P(dev(Fp)), P(p2g), P(r2g), float(dh2), NX, NZ)
+    L.SecondDerivate_P_h(P(D(Pp)), P(D(Fp)), P(p2g), P(r2g), float(dh2), NX, NZ)
     assert tol(host(p2g), p2o) and tol(host(r2g), r2o)
     # PSI_F
     a_o, b_o = psx.copy(), psz.copy()
     O.orc_psi_f_f32(ptr(Pp), ptr(Fp), ptr(ax), ptr(bx), ptr(az), ptr(bz), ptr(a_o), ptr(b_o), NX, NZ, DH, CPML)
     a_g, b_g = dev(psx), dev(psz)
-    L.PSI_F_h(P(dev(Pp)), P(dev(Fp)), P(dev(ax)), P(dev(bx)), P(dev(az)), P(dev(bz)), P(a_g), P(b_g), NX, NZ,
+    L.PSI_F_h(P(D(Pp)), P(D(Fp)), P(D(ax)), P(D(bx)), P(D(az)), P(D(bz)), P(a_g), P(b_g), NX, NZ,
               DH, CPML)
     assert tol(host(a_g), a_o) and tol(host(b_g), b_o)
     # ZETA_F (on the oracle's p2/r2/psi)
@@ -204,8 +215,8 @@ def test_single_step_kernels_against_oracle(L):
     O.orc_zeta_f_f32(ptr(p2o), ptr(r2o), ptr(ax), ptr(bx), ptr(az), ptr(bz), ptr(a_o), ptr(b_o), ptr(zx_o),
                      ptr(zz_o), ptr(ap_o), ptr(af_o), NX, NZ, DH, CPML)
     zx_g, zz_g, ap_g, af_g = dev(zx), dev(zz), zeros(NZ, NX), zeros(NZ, NX)
-    L.ZETA_F_h(P(dev(p2o)), P(dev(r2o)), 0, 0, P(dev(ax)), P(dev(bx)), P(dev(az)), P(dev(bz)), P(dev(a_o)),
-               P(dev(b_o)), P(zx_g), P(zz_g), P(ap_g), P(af_g), NX, NZ, DH, float(dh2), CPML)
+    L.ZETA_F_h(P(D(p2o)), P(D(r2o)), 0, 0, P(D(ax)), P(D(bx)), P(D(az)), P(D(bz)), P(D(a_o)),
+               P(D(b_o)), P(zx_g), P(zz_g), P(ap_g), P(af_g), NX, NZ, DH, float(dh2), CPML)
     for g_, o_ in ((zx_g, zx_o), (zz_g, zz_o), (ap_g, ap_o), (af_g, af_o)):
         assert tol(host(g_), o_)
     # propagator_F (source and receivers on row sz-1)
@@ -214,8 +225,8 @@ def test_single_step_kernels_against_oracle(L):
                            ptr(vp), ptr(vn), ptr(ap_o), ptr(af_o), ptr(src), ptr(shot_o), C_, dh2, NX, NZ,
                            21, SZ, 40, CPML)
     Pn_g, Fn_g, PF_g, shot_g = dev(Pq), dev(Fq), zeros(NZ, NX), zeros(NT, NX)
-    L.propagator_F_h(P(dev(p2o)), P(dev(r2o)), P(PF_g), P(dev(Pp)), P(dev(Fp)), P(Pn_g), P(Fn_g), P(dev(vh)),
-                     P(dev(vp)), P(dev(vn)), P(dev(ap_o)), P(dev(af_o)), P(dev(src)), P(shot_g), float(C_),
+    L.propagator_F_h(P(D(p2o)), P(D(r2o)), P(PF_g), P(D(Pp)), P(D(Fp)), P(Pn_g), P(Fn_g), P(D(vh)),
+                     P(D(vp)), P(D(vn)), P(D(ap_o)), P(D(af_o)), P(D(src)), P(shot_g), float(C_),
                      float(dh2), NX, NZ, 21, SZ, 40, CPML)
     for g_, o_ in ((Pn_g, Pn_o), (Fn_g, Fn_o), (PF_g, PF_o), (shot_g, shot_o)):
         assert tol(host(g_), o_)
@@ -224,7 +235,7 @@ def test_single_step_kernels_against_oracle(L):
     ro = np.zeros_like(s1)
     O.orc_res_f32(ptr(ro), ptr(s1), ptr(s2), NX, NZ)
     rg = zeros(NZ, NX)
-    L.res_h(P(rg), P(dev(s1)), P(dev(s2)), NX, NZ)
+    L.res_h(P(rg), P(D(s1)), P(D(s2)), NX, NZ)
     assert np.array_equal(host(rg), ro)
     assert L.fwi_compat_last_error() == 0
 

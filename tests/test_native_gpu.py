@@ -269,3 +269,24 @@ def test_errors_are_reported_not_faulted():
     too_long = make_shots([(20, SZ - 1, SZ - 1, CPML, NX - CPML, NT + 1)])
     with pytest.raises(FwiError):
         ctx.forward(too_long)
+
+
+@pytest.mark.parametrize("mode", ["exact", "ref"])
+@pytest.mark.parametrize("every,sprec", [(1, 0), (37, 0), (64, 1), (0, 2), (260, 0)])
+def test_checkpointing_reproduces_full_storage_bitwise(exact_case, mode, every, sprec):
+    """Segments recomputed from checkpoints give the images a full store keeps,
+    so the gradient is bit-identical (uneven nt and windows included)."""
+    from fwi_gb300 import Context, MODE_EXACT, MODE_REF_COMPAT, PREC_FP32, STORE_CHECKPOINT, STORE_FULL, make_shots
+    p, shots, obs, mask, _, _ = exact_case
+    res = []
+    for store in (STORE_FULL, STORE_CHECKPOINT):
+        ctx = Context(nx=p["nx"], nz=p["nz"], dh=p["dh"], dt=p["dt"], cpml=p["cpml"], f_cpml=p["f"],
+                      nt_max=p["nt"], max_shots=2, mode=MODE_EXACT if mode == "exact" else MODE_REF_COMPAT,
+                      precision=PREC_FP32, store=store, store_prec=sprec, ckpt_every=every)
+        ctx.set_wavelet(wavelet(p).astype(np.float32))
+        ctx.set_model(*(np.ascontiguousarray(p[k], np.float32) for k in ("vh", "vp", "vn")))
+        res.append(ctx.gradient(make_shots(shots), obs.astype(np.float32), mask))
+        del ctx
+    assert res[0][0] == res[1][0]
+    for a, b in zip(res[0][1:], res[1][1:]):
+        assert np.array_equal(a, b)

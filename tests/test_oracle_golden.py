@@ -118,8 +118,8 @@ def test_update_lbfgs_with_and_without_clamps_bitexact():
     r = [G["lb0_r_b1"], G["lb0_r_b2"], G["lb0_r_b3"]]
     for alpha, fmin, fmax, tag in ((1.0, 0, 0, "2"), (40.0, 1, 1, "3")):
         vp, vn, vh = G["vp_1"].copy(), G["vn_1"].copy(), G["vh_1"].copy()
-        L.orc_update_lbfgs_f32(P(r[0]), P(r[1]), P(r[2]), P(vp), P(vn), P(vh), P(G["vp_i"]),
-                               P(G["vn_i"]), P(G["vh_i"]), nx, nz, alpha, alpha, alpha, 1, 1, 1,
+        L.orc_update_lbfgs_f32(P(r[0]), P(r[1]), P(r[2]), P(vp), P(vn), P(vh), P(G["vp_1"]),
+                               P(G["vn_1"]), P(G["vh_1"]), nx, nz, alpha, alpha, alpha, 1, 1, 1,
                                fmin, fmax)
         assert np.array_equal(vp, G[f"vp_{tag}"]) and np.array_equal(vn, G[f"vn_{tag}"])
         assert np.array_equal(vh, G[f"vh_{tag}"])
