@@ -124,10 +124,14 @@ __global__ void __launch_bounds__(kStripBlock) k_fwd_strip(Batch<T> b, int g, in
     }
 }
 
-template <typename T, int ST, bool EXACT, bool STORE>
+// `img_slot` < 0: no images this step.  A runtime flag, not a template
+// parameter, so that passes with and without images execute the same
+// arithmetic (a checkpointed segment must recompute the state bit for bit).
+template <typename T, int ST, bool EXACT>
 __global__ void __launch_bounds__(PTX * PBY)
 k_fwd_main(Batch<T> b, int g, int ntb, int cur, int img_slot)
 {
+    const bool STORE = img_slot >= 0;
     using Cd = Codec<T, ST>;
     const int s = blockIdx.z;
     const DevShot sh = b.shots[s];
@@ -503,18 +507,11 @@ inline dim3 strip_grid(const Batch<T> &b, int nx_max)
     return dim3((unsigned)blocks, b.B);
 }
 
-template <typename T, int ST, bool EXACT, bool STORE>
-inline void fwd_main_launch(const Batch<T> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
-{
-    k_fwd_main<T, ST, EXACT, STORE><<<main_grid(b, nx_max), dim3(PTX, PBY), 0, st>>>(b, g, ntb, cur, slot);
-}
-
 template <typename T, int ST>
 inline void fwd_dispatch(const Batch<T> &b, int nx_max, int g, int ntb, int cur, int slot, bool exact, cudaStream_t st)
 {
-    if (slot < 0) fwd_main_launch<T, ST, false, false>(b, nx_max, g, ntb, cur, 0, st);
-    else if (exact) fwd_main_launch<T, ST, true, true>(b, nx_max, g, ntb, cur, slot, st);
-    else fwd_main_launch<T, ST, false, true>(b, nx_max, g, ntb, cur, slot, st);
+    if (exact) k_fwd_main<T, ST, true><<<main_grid(b, nx_max), dim3(PTX, PBY), 0, st>>>(b, g, ntb, cur, slot);
+    else k_fwd_main<T, ST, false><<<main_grid(b, nx_max), dim3(PTX, PBY), 0, st>>>(b, g, ntb, cur, slot);
 }
 
 template <typename T>

@@ -289,4 +289,4 @@ def test_checkpointing_reproduces_full_storage_bitwise(exact_case, mode, every, 
         del ctx
     assert res[0][0] == res[1][0]
     for a, b in zip(res[0][1:], res[1][1:]):
-        assert np.array_equal(a, b)
+        assert np.array_equal(a, b), rel_l2(b, a)
