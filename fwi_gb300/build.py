@@ -21,7 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libfwi_gb300.so")
 
-UNITS = ["compat.cu", "native.cu", "prop_f32.cu", "prop_f64.cu"]
+UNITS = ["compat.cu", "native.cu", "prop_f32.cu", "prop_f64.cu", "noalloc.cu"]
 HEADERS = ["common.cuh", "tile.cuh", "prop.h", "prop.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

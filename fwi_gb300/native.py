@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_last_timing", [_p, _p])
         _sig(L, "fwi_last_launches", [_p], _l)
         _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
+        _sig(L, "fwi_residual_misfit_noalloc", [_p, _p, _p, _p, _l, _i, _p, _p])
         # reference-compatible ABI: float* device pointers, ints, floats
         _sig(L, "pre_variables_h", [_p] * 6 + [_i, _i], None)
         _sig(L, "CPML_x_h", [_p, _p, _i, _f, _i, _f, _f, _f, _f, _f], None)

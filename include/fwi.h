@@ -168,6 +168,27 @@ int fwi_last_timing(void *ctx, float *out4);
 /* How many of this library's kernels the last call launched. */
 long fwi_last_launches(void *ctx);
 
+/* ---- residual and misfit without device allocation ----
+ * No counterpart in the reference (it copies the residual to the host and sums it there,
+ * src/main.c:437-454).  For callers that cannot let the library allocate device memory:
+ * drivers shaped like src/main.c that allocate every buffer once before the shot loop, or
+ * processes whose device memory is owned by another allocator with a fixed budget.
+ * res = mask (syn - obs) over an [nt][nrec] block of FP32 traces (mask: [nrec] bytes,
+ * 0 = dropped trace, or NULL) and *misfit = 1/2 sum res^2 accumulated in FP64, in a fixed
+ * order.  All pointers are device pointers (misfit: one double); the work is ordered on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and nothing is waited for.
+ * Scratch is a fixed array inside the library (FWI_NOALLOC_MAX_BLOCKS + 1 doubles per
+ * device, held until the process exits); it limits nt * nrec to FWI_NOALLOC_MAX_ELEMENTS
+ * (larger requests return FWI_ERR_ARG).  Every call shares that array, so calls that
+ * overlap on the GPU (other streams, other threads) race; serialise them.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture. */
+#define FWI_NOALLOC_MAX_BLOCKS 16384
+#define FWI_NOALLOC_MAX_ELEMENTS (16384L * 4096L)
+int fwi_residual_misfit_noalloc(float *res, const float *syn, const float *obs,
+                                const unsigned char *mask, long nt, int nrec, double *misfit,
+                                void *stream);
+
 /* Host-side helper, no GPU needed: the CPML strip points of an nx x nz grid
  * (the points src/parallelcalls.cu:55 updates), in the order the strip kernels
  * visit them.  Returns the count; writes at most cap pairs. */
