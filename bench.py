@@ -247,7 +247,7 @@ def native_arm(args, rank, world, dist):
             sum((s["nxw"] or w.nx) * w.nz * s["nt"] for s in w.shots)
         adj_gbs = ALG_BYTES_ADJ * pts / (t_adj / args.steps / 1e3) / 1e9
         fwd_gbs = ALG_BYTES_FWD * pts / (t_fwd / args.steps / 1e3) / 1e9
-        traffic = traffic_from_profile(f"k_adj_main_{args.workload}_traffic.txt")
+        traffic = traffic_from_profile(f"adjoint_step_{args.workload}_traffic.txt")
         launches_per_step = 2 * w.nt
         out = {
             "metric": METRIC, "value": round(value, 4), "unit": "shots/s", "n_gpus": world,
@@ -261,7 +261,7 @@ def native_arm(args, rank, world, dist):
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
                     "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
-            "roofline": {"bound": "hbm", "kernel": "adjoint step (k_adj_strip + k_adj_main)",
+            "roofline": {"bound": "hbm", "kernel": "adjoint step (k_adj_strip_exact + k_adj_tma + k_adj_cpml)",
                          "achieved": round(adj_gbs, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(adj_gbs / hbm, 4), "peak_kind": peak_kind,
                          "traffic": traffic, "forward_step_achieved": round(fwd_gbs, 1),

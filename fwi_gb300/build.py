@@ -22,7 +22,8 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libfwi_gb300.so")
 
 UNITS = ["compat.cu", "native.cu", "prop_f32.cu", "prop_f64.cu", "noalloc.cu"]
-HEADERS = ["common.cuh", "tile.cuh", "prop.h", "prop.cuh"]
+HEADERS = ["common.cuh", "tile.cuh", "prop.h", "prop.cuh", "prop_tma.cuh", "tma.cuh"]
+C_UNITS = ["driver.c"]  # host C over the C-ABI
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -62,6 +63,14 @@ def build(force: bool = False, jobs: int = 4, verbose: bool = False) -> str:
         if p.returncode != 0:
             raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{p.stdout}\n{p.stderr}")
         return p
+
+    cc = os.environ.get("CC", "gcc")
+    for u in C_UNITS:
+        src = os.path.join(CSRC, u)
+        obj = os.path.join(BUILD, u.replace(".c", ".o"))
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            todo.append([cc, "-O2", "-fPIC", "-std=c11", "-Wall", "-I", inc, "-c", src, "-o", obj])
 
     with ThreadPoolExecutor(max_workers=max(1, jobs)) as ex:
         list(ex.map(run, todo))

@@ -11,6 +11,7 @@
 #include "../../include/fwi.h"
 #include "common.cuh"
 #include "prop.h"
+#include "tma.cuh"
 
 #include <cuda_fp16.h>
 
@@ -19,6 +20,51 @@
 #include <cstdio>
 #include <cstring>
 #include <vector>
+
+namespace fwi {
+
+EncodeTiledFn tensor_map_encoder()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+int make_tensor_map_3d(CUtensorMap *map, const void *base, CUtensorMapDataType type, int elem, long pitch,
+                       long rows, long depth, int bx, int by, int bz)
+{
+    EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc) return FWI_ERR_NODEVICE;
+    cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)rows, (cuuint64_t)depth};
+    cuuint64_t strides[2] = {(cuuint64_t)(pitch * elem), (cuuint64_t)(pitch * rows * elem)};
+    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(map, type, 3, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? FWI_OK : FWI_ERR_CUDA;
+}
+
+// Mirrors the layout of fwi::TmaMaps in prop_tma.cuh (device code is not
+// compiled into this unit).
+struct HostTmaMaps {
+    CUtensorMap lvl[4];
+    CUtensorMap inc[2];
+    CUtensorMap img;
+};
+
+}  // namespace fwi
 
 namespace {
 
@@ -129,20 +175,23 @@ __global__ void k_misfit_finish(const double *partial, long n, double *misfit)
     }
 }
 
-// grad[iz][X] += sum over the batch's shots of their local gradients (fixed shot order).
+// grad[iz][X] += sum over the batch's shot groups of their local gradients
+// (fixed group order); group q holds shots [q sg, (q+1) sg), all with the
+// window of shot q sg.
 template <typename T>
 __global__ void k_accumulate_gradient(T *gh, T *gp, T *gn, const T *sh_h, const T *sh_p, const T *sh_n,
-                                      const DevShot *shots, int B, int nx, int nz, int mpitch, int pitch,
-                                      long slot)
+                                      const DevShot *shots, int ngroups, int sg, int nx, int nz, int mpitch,
+                                      int pitch, long slot)
 {
     const long n = (long)nx * nz;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
         const int iz = (int)(k / nx), X = (int)(k - (long)iz * nx);
         T a = T(0), b = T(0), c = T(0);
-        for (int s = 0; s < B; s++) {
-            const int lx = X - shots[s].x0;
-            if (lx < 0 || lx >= shots[s].nx) continue;
-            const long i = (long)s * slot + (long)iz * pitch + lx;
+        for (int q = 0; q < ngroups; q++) {
+            const DevShot &w = shots[q * sg];
+            const int lx = X - w.x0;
+            if (lx < 0 || lx >= w.nx) continue;
+            const long i = (long)q * slot + (long)iz * pitch + lx;
             a += sh_h[i];
             b += sh_p[i];
             c += sh_n[i];
@@ -386,6 +435,7 @@ struct CtxBase {
     virtual int get_model(void *, void *, void *) = 0;
     virtual int set_wavelet(const void *, int) = 0;
     virtual int set_ricker(float, int) = 0;
+    virtual int set_frequency(float, int) = 0;
     virtual int run(const fwi_shot *, int, const void *, const unsigned char *, void *, void *, void *,
                     double *, void *traces, bool grad) = 0;
     virtual int first_step(float, float, float) = 0;
@@ -421,12 +471,15 @@ template <typename T> struct Ctx : CtxBase {
     bool have_model = false, have_wavelet = false, models_dirty = true;
     int wavelet_nt = 0;
     // batch
-    T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {};
+    T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {}, *scr[4] = {};
     void *store = nullptr;
     // checkpointing: full states every ck_every steps, segment recompute buffers
     int ck_every = 0, n_ck = 0;
     T *ck = nullptr;                 // [n_ck][8][B * slot]: P, F, their increments, CPML x4
     T *rlvl[6] = {}, *rcp[4] = {};
+    // TMA tensor maps of the batch buffers and of the recompute buffers (FP32 contexts)
+    fwi::HostTmaMaps maps{}, rmaps{};
+    bool use_tma = false;
     float *scale = nullptr, *amax = nullptr;
     T *rec = nullptr, *obs = nullptr;
     unsigned char *mask = nullptr;
@@ -494,6 +547,7 @@ template <typename T> struct Ctx : CtxBase {
         for (auto &p : lvl) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : cp) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : gs) TRY(alloc(&p, (size_t)B * slot));
+        for (auto &p : scr) TRY(alloc(&p, (size_t)B * slot));
         if (cfg.store == FWI_STORE_CHECKPOINT) {
             ck_every = checkpoint_interval(cfg);
             n_ck = (nt_max + ck_every - 1) / ck_every;
@@ -507,6 +561,12 @@ template <typename T> struct Ctx : CtxBase {
             TRY(cudaMalloc(&q0, (size_t)B * n_img * 2 * slot * store_elem()));
             allocs.push_back(q0);
             store = q0;
+        }
+        if (sizeof(T) == sizeof(float)) {
+            int rc = build_maps(maps, lvl) ;
+            if (rc == FWI_OK && cfg.store == FWI_STORE_CHECKPOINT) rc = build_maps(rmaps, rlvl);
+            if (rc != FWI_OK) return rc;
+            use_tma = true;
         }
         TRY(alloc(&scale, (size_t)B * nt_max));
         TRY(alloc(&amax, (size_t)B * (nt_max + 1)));
@@ -527,14 +587,63 @@ template <typename T> struct Ctx : CtxBase {
         TRY(cudaMemsetAsync(ds.counter, 0, sizeof(unsigned), st));
         TRY(cudaMemsetAsync(lbs, 0, sizeof(LbScalars), st));
         for (T *p : {vh, vp, vn, mh, mp, mn}) TRY(cudaMemsetAsync(p, 0, mslot * sizeof(T), st));
-        // CPML table by distance (src/main.c:48-51: L = CPML dh, d0 = -3 ln R / (2 L), in T)
+        int rcc = cpml_table();
+        if (rcc) return rcc;
+        TRY_LAUNCH();
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int build_maps(fwi::HostTmaMaps &m, T *const (&lv)[6])
+    {
+        using namespace fwi;
+        for (int k = 0; k < 4; k++) {
+            int rc = make_tensor_map_3d(&m.lvl[k], lv[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 40, 40, 1);
+            if (rc) return rc;
+        }
+        for (int k = 0; k < 2; k++) {
+            int rc = make_tensor_map_3d(&m.inc[k], lv[4 + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 32, 32, 1);
+            if (rc) return rc;
+        }
+        const int st_t = store_type();
+        const CUtensorMapDataType it = st_t == kStoreHalf ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                       : st_t == kStoreBf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                                            : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        return make_tensor_map_3d(&m.img, store, it, (int)store_elem(), pitch, nz, (long)B * n_img * 2, 32, 32, 2);
+    }
+
+    // Shots per group for a batch: groups need identical windows; with them,
+    // enough groups to give about four blocks per SM.
+    int shots_per_group(const std::vector<DevShot> &bs, int nxm) const
+    {
+        if (!use_tma) return 1;
+        for (const DevShot &d : bs)
+            if (d.x0 != bs[0].x0 || d.nx != bs[0].nx) return 1;
+        const long tiles = (long)((nxm + 31) / 32) * ((nz + 31) / 32);
+        const int nb = (int)bs.size();
+        long groups = std::max<long>(1, std::min<long>(nb, (4L * 152 + tiles - 1) / tiles));
+        int sg = (int)((nb + groups - 1) / groups);
+        return std::max(1, std::min(sg, 64));
+    }
+
+    // CPML table by distance (src/main.c:48-51: L = CPML dh, d0 = -3 ln R / (2 L), in T)
+    int cpml_table()
+    {
         const T L = cfg.cpml * (T)cfg.dh;
         const T d0 = (T)(-3 * log((double)cfg.r_coef) / (double)(2 * L));
         k_cpml_table<T><<<(cfg.cpml + 128) / 128, 128, 0, st>>>(cpa, cpb, cfg.cpml, (T)cfg.vmax, (T)cfg.dt,
                                                                  (T)cfg.dh, (T)cfg.f_cpml, d0, L);
         TRY_LAUNCH();
-        TRY(cudaStreamSynchronize(st));
         return FWI_OK;
+    }
+
+    int set_frequency(float f, int nt) override
+    {
+        if (!(f > 0) || nt <= 0 || nt > nt_max) return FWI_ERR_ARG;
+        cfg.f_cpml = f;
+        int rc = cpml_table();
+        if (rc) return rc;
+        return set_ricker(f, nt);
     }
 
     int copy_model_in(T *dst, const void *src)
@@ -646,6 +755,7 @@ template <typename T> struct Ctx : CtxBase {
         for (int k = 0; k < 6; k++) b.lvl[k] = lvl[k];
         for (int k = 0; k < 8; k++) b.cp[k] = cp[k];
         for (int k = 0; k < 3; k++) b.g[k] = gs[k];
+        for (int k = 0; k < 4; k++) b.scr[k] = scr[k];
         b.store = store; b.store_type = store_type(); b.n_img = n_img;
         b.scale = scale; b.amax = amax; b.rec = rec; b.shots = shots;
         b.mh = mh; b.mp = mp; b.mn = mn; b.cpa = cpa; b.cpb = cpb; b.wavelet = wavelet;
@@ -653,6 +763,8 @@ template <typename T> struct Ctx : CtxBase {
         b.inv_dh2 = T(1) / ((T)cfg.dh * (T)cfg.dh);
         b.img_scale = cfg.mode == FWI_MODE_EXACT ? (T)cfg.dt * (T)cfg.dt : (T)cfg.dt;
         b.status = status;
+        b.sg = 1;
+        b.tma = use_tma ? (const void *)&maps : nullptr;
         return b;
     }
 
@@ -671,6 +783,10 @@ template <typename T> struct Ctx : CtxBase {
         T *dst[8] = {rlvl[cur], rlvl[2 + cur], rlvl[4], rlvl[5], rcp[0], rcp[1], rcp[2], rcp[3]};
         for (int a = 0; a < 8; a++)
             TRY(cudaMemcpyAsync(dst[a], ck + ((size_t)k * 8 + a) * B * slot, bytes, cudaMemcpyDeviceToDevice, st));
+        // a shot that starts later inside the segment reads the other level when it starts:
+        // give both levels the checkpointed state (zero for such a shot)
+        TRY(cudaMemcpyAsync(rlvl[1 - cur], ck + ((size_t)k * 8 + 0) * B * slot, bytes, cudaMemcpyDeviceToDevice, st));
+        TRY(cudaMemcpyAsync(rlvl[3 - cur], ck + ((size_t)k * 8 + 1) * B * slot, bytes, cudaMemcpyDeviceToDevice, st));
         return FWI_OK;
     }
 
@@ -722,6 +838,8 @@ template <typename T> struct Ctx : CtxBase {
             for (int k = 0; k < 4; k++) TRY(cudaMemsetAsync(cp[k], 0, lb, st));
             TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
             Batch<T> b = batch_view(nb);
+            b.sg = shots_per_group(bs, nxm);
+            const int ngroups = (nb + b.sg - 1) / b.sg;
             cudaEvent_t e0 = ev[1], e1 = ev[2], e2 = ev[3];
             TRY(cudaEventRecord(e0, st));
             const bool ckpt = want_grad && cfg.store == FWI_STORE_CHECKPOINT;
@@ -769,6 +887,9 @@ template <typename T> struct Ctx : CtxBase {
                     for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
                     for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
                     for (int k = 0; k < 4; k++) rb.cp[k] = rcp[k];
+                    rb.tma = use_tma ? (const void *)&rmaps : nullptr;
+                    // `rec` holds the residuals now; the recomputed traces go to the spent obs copy
+                    rb.rec = obs;
                     int j = 0;
                     for (int seg = (ntb - 1) / ck_every; seg >= 0; seg--) {
                         const int a = seg * ck_every, e = std::min(a + ck_every, ntb);
@@ -796,7 +917,8 @@ template <typename T> struct Ctx : CtxBase {
                     TRY_LAUNCH();
                 }
                 k_accumulate_gradient<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(
-                    grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, nb, nx, nz, mpitch, pitch, slot);
+                    grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, ngroups, b.sg, nx, nz, mpitch, pitch,
+                    slot);
                 TRY_LAUNCH();
                 launches++;
             }
@@ -832,7 +954,8 @@ template <typename T> struct Ctx : CtxBase {
         timing[2] = t_adj;
         timing[3] = tot - t_fwd - t_adj;
         launches = launches - launches0;
-        if (stat & 1u) return FWI_ERR_NUMERIC;
+        if (stat & fwi::kStatusTimeout) return FWI_ERR_CUDA;
+        if (stat & fwi::kStatusSaturated) return FWI_ERR_NUMERIC;
         if (misfit_out && !std::isfinite(*misfit_out)) return FWI_ERR_NUMERIC;
         return FWI_OK;
     }
@@ -1040,7 +1163,7 @@ size_t fwi_config_bytes(const fwi_config *c)
     const long nrec = c->max_receivers > 0 ? c->max_receivers : win;
     size_t b = 0;
     b += (size_t)(6 + 3 + 12) * mslot * e;                 // models, gradient, L-BFGS work arrays
-    b += (size_t)c->max_shots * slot * e * (6 + 8 + 3);    // levels, CPML state, per-shot gradients
+    b += (size_t)c->max_shots * slot * e * (6 + 8 + 3 + 4); // levels, CPML state, gradients, scratch
     if (c->store == FWI_STORE_CHECKPOINT) {
         const long k = checkpoint_interval(*c), n = (c->nt_max + k - 1) / k;
         b += (size_t)c->max_shots * slot * e * (8 * n + 10); // checkpoints, recompute state
@@ -1112,6 +1235,7 @@ int fwi_set_model_vti(void *ctx, const void *a, const void *b, const void *c)
 int fwi_get_model(void *ctx, void *a, void *b, void *c) { return ctx ? as_ctx(ctx)->get_model(a, b, c) : FWI_ERR_ARG; }
 int fwi_set_wavelet(void *ctx, const void *w, int nt) { return ctx ? as_ctx(ctx)->set_wavelet(w, nt) : FWI_ERR_ARG; }
 int fwi_set_ricker(void *ctx, float f, int nt) { return ctx ? as_ctx(ctx)->set_ricker(f, nt) : FWI_ERR_ARG; }
+int fwi_set_frequency(void *ctx, float f, int nt) { return ctx ? as_ctx(ctx)->set_frequency(f, nt) : FWI_ERR_ARG; }
 
 int fwi_forward(void *ctx, const fwi_shot *shots, int n, void *traces)
 {

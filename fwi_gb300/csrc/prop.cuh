@@ -46,7 +46,7 @@ template <typename T> struct Codec<T, kStoreNative> {
     using S = T;
     static constexpr bool scaled = false;
     static __device__ __forceinline__ S enc(T v, float, unsigned *) { return v; }
-    static __device__ __forceinline__ T dec(S v, float) { return v; }
+    static __device__ __forceinline__ T dec(S v, float) { return v; }  // second argument: inverse scale
 };
 template <typename T> struct Codec<T, kStoreHalf> {
     using S = __half;
@@ -60,24 +60,27 @@ template <typename T> struct Codec<T, kStoreHalf> {
         }
         return __float2half_rn(x);
     }
-    static __device__ __forceinline__ T dec(S v, float sc) { return (T)(__half2float(v) / sc); }
+    static __device__ __forceinline__ T dec(S v, float inv_sc) { return (T)(__half2float(v) * inv_sc); }
 };
 template <typename T> struct Codec<T, kStoreBf16> {
     using S = __nv_bfloat16;
     static constexpr bool scaled = true;
     static __device__ __forceinline__ S enc(T v, float sc, unsigned *) { return __float2bfloat16_rn((float)v * sc); }
-    static __device__ __forceinline__ T dec(S v, float sc) { return (T)(__bfloat162float(v) / sc); }
+    static __device__ __forceinline__ T dec(S v, float inv_sc) { return (T)(__bfloat162float(v) * inv_sc); }
 };
 
 // Per-snapshot scale: a power of two that maps the largest possible image
 // value of the step to about 2^14.  |G|, |H| <= 32 max(|P|,|F|) / dh^2 for
 // the 8th-order operator plus the CPML terms (|a| / (1 - b) <= 1), so the
-// bound comes from the state's max, which the previous step recorded.
+// bound comes from the state's max, which the previous step recorded.  Made
+// with ldexpf so that it and its inverse are exact powers of two: decoding
+// multiplies by the inverse and gets the same value a division would.
 __device__ __forceinline__ float image_scale(float amax, float inv_dh2)
 {
-    float bound = 32.f * amax * inv_dh2;
+    const float bound = 32.f * amax * inv_dh2;
     if (!(bound > 0.f) || !isfinite(bound)) return 1.f;
-    return exp2f(floorf(log2f(16384.f / bound)));
+    const float e = floorf(log2f(16384.f / bound));
+    return ldexpf(1.f, (int)fminf(fmaxf(e, -120.f), 120.f));
 }
 
 __device__ __forceinline__ void block_max_to(float v, float *dst)
@@ -386,10 +389,10 @@ k_adj_main(Batch<T> b, int j, int ntb, int cur, int zsel, int img_base)
     const int img_local = m - 1 - lag;
     const int img_g = ntb - 1 - lag - j;
     const typename Cd::S *img = nullptr;
-    float sc = 1.f;
+    float inv_sc = 1.f;
     if (img_local >= 0) {
         img = (const typename Cd::S *)b.store + ((long)s * b.n_img + (img_g - img_base)) * 2 * b.slot;
-        if (Cd::scaled) sc = b.scale[(long)s * b.nt_max + img_g];
+        if (Cd::scaled) inv_sc = 1.f / b.scale[(long)s * b.nt_max + img_g];
     }
     const int nrec = sh.rx1 - sh.rx0;
     const T *res_row = b.rec + sh.rec_off + (long)(m - 1) * nrec;
@@ -480,7 +483,7 @@ k_adj_main(Batch<T> b, int j, int ntb, int cur, int zsel, int img_base)
         lPn[i] = pn;
         lFn[i] = fn;
         if (img) {
-            const T G = Cd::dec(img[i], sc), H = Cd::dec(img[b.slot + i], sc);
+            const T G = Cd::dec(img[i], inv_sc), H = Cd::dec(img[b.slot + i], inv_sc);
             const T k = b.img_scale;
             g0[i] += k * G * pn;
             g1[i] += k * H * (pn + fn);

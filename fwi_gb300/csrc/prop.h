@@ -26,6 +26,7 @@ template <typename T> struct Batch {
     T *lvl[6];      // P level 0, P level 1, F level 0, F level 1, P increment, F increment
     T *cp[8];       // CPML memory variables (forward uses 0..3)
     T *g[3];        // per-shot gradient accumulators: v_hor, v_po, v_nmo
+    T *scr[4];      // per-shot scratch: stencil values the tile kernels hand to the layer kernels
     void *store;    // images: [B][n_img][2][slot] of the store type
     int store_type; // StoreType
     int n_img;      // image slots per shot
@@ -38,7 +39,10 @@ template <typename T> struct Batch {
     const T *wavelet;
     T inv_dh, inv_dh2;
     T img_scale;            // dt (reference imaging) or dt^2 (exact)
-    unsigned *status;       // bit 0: stored image saturated
+    unsigned *status;       // bit 0: stored image saturated, bit 1: a pipeline wait gave up
+    int sg;                 // shots per group: shots [q sg, (q+1) sg) share a window, and
+                            // g[k] + q * slot accumulates the imaging of group q
+    const void *tma;        // host copy of the batch's TMA tensor maps (FP32 path), or null
 };
 
 // Shots of a batch run end-aligned on one global clock of `ntb` steps (the

@@ -1,0 +1,797 @@
+// FP32 main passes (sm_103a): TMA tile loads, shot groups, 4-wide vectors.
+//
+// Per time step:
+//  * tile kernels (k_fwd_tma, k_adj_tma): one block per 32x32 tile loops over
+//    a group of shots that share a window; each shot's tiles (the two stencil
+//    fields with a 4-point halo, the increments, the images) arrive by
+//    cp.async.bulk.tensor into one of two shared-memory stages while the
+//    block computes the previous shot (2-stage mbarrier pipeline, one issuing
+//    thread).  A thread owns 4 consecutive points of a row: the x-stencil is 3
+//    ld.shared.v4, the z-stencil 9, stores are 16-byte vectors.  Points the
+//    CPML layers do not touch are finished here; for the others the block
+//    only writes the stencil values it already has to per-shot scratch.  The
+//    adjoint sums the imaging of its group in registers (one gradient
+//    read-modify-write per group and step).
+//  * layer kernels (k_fwd_cpml, k_adj_cpml): the points inside the layers
+//    (forward, reference adjoint) or within 4 points of them (exact adjoint,
+//    whose transpose terms reach that far): memory-variable terms, update,
+//    receivers and imaging, from the scratch stencil values.
+#pragma once
+
+#include "prop.cuh"
+#include "tma.cuh"
+
+namespace fwi {
+
+constexpr int TT = 32;             // tile edge
+constexpr int TH = TT + 2 * kRad;  // tile with a 4-point halo on every side (40)
+constexpr int kTmaThreads = 256;   // 8 threads x 4 points per row, 32 rows
+constexpr int kMaxGroup = 64;
+
+// Tensor maps over one batch's per-shot arrays ([B][nz][pitch]) and images.
+struct TmaMaps {
+    CUtensorMap lvl[4];  // P level 0/1, F level 0/1: 40 x 40 boxes
+    CUtensorMap inc[2];  // P and F increments: 32 x 32 boxes
+    CUtensorMap img;     // images [B * n_img * 2][nz][pitch]: 32 x 32 x 2 boxes
+};
+
+struct FwdStage {
+    float P[TH][TH];
+    float F[TH][TH];
+    float Pv[TT][TT];
+    float Fv[TT][TT];
+};
+
+template <typename S> struct AdjStage {
+    float P[TH][TH];
+    float F[TH][TH];
+    float Pw[TT][TT];
+    float Fw[TT][TT];
+    S I[2][TT][TT];
+};
+
+// Points the layers touch: those are left to the point-list kernels.  `aw`
+// is the CPML width (forward, reference adjoint) or CPML width + 4 (exact
+// adjoint).  Same shape as the reference's strip predicate.
+__device__ __forceinline__ bool layer_point(int ix, int iz, int nx, int nz, int aw)
+{
+    return ix < aw || ix > nx - aw - 1 || iz > nz - aw - 1;
+}
+
+__device__ __forceinline__ unsigned char *aligned_dsm(unsigned char *p)
+{
+    const uint32_t a = smem_addr(p);
+    return p + ((128u - (a & 127u)) & 127u);
+}
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ float comp(const float4 &v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+
+// Bounded wait whose outcome every thread of the block agrees on.  Thread 0
+// polls; the other threads sleep in the barrier and then observe the
+// completed phase themselves with one more try_wait (which returns at once),
+// so that the staged data is visible to each of them.
+__device__ __forceinline__ bool stage_ready(uint64_t *bar, unsigned parity, unsigned *status)
+{
+    bool ok = true;
+    if (threadIdx.x == 0) ok = mbar_wait(bar, parity);
+    const bool any_fail = __syncthreads_or(!ok);
+    if (any_fail) {
+        if (threadIdx.x == 0) atomicOr(status, kStatusTimeout);
+        return false;
+    }
+    if (threadIdx.x != 0) (void)mbar_wait(bar, parity);
+    return true;
+}
+
+// After a failed wait: give the loads still in flight a bounded time to land
+// before the block's shared memory is released.
+__device__ __forceinline__ void drain_stage(uint64_t *bar, unsigned parity)
+{
+    if (threadIdx.x == 0) (void)mbar_wait(bar, parity);
+    __syncthreads();
+}
+
+__device__ __forceinline__ int active_shots(const Batch<float> &b, int sg, int *act, bool adjoint, int step, int ntb)
+{
+    __shared__ int n_s;
+    if (threadIdx.x == 0) {
+        const int s0 = blockIdx.z * sg, s1 = min(s0 + sg, b.B);
+        int n = 0;
+        for (int s = s0; s < s1; s++) {
+            const int nt = b.shots[s].nt;
+            if (adjoint ? (step < nt) : (step - (ntb - nt) >= 0)) act[n++] = s;
+        }
+        n_s = n;
+    }
+    __syncthreads();
+    return n_s;
+}
+
+// 8th-order second derivative (unnormalised, difference form) of 4
+// consecutive points from 12 values v[0..11] = f(ix0 - 4 .. ix0 + 7).
+__device__ __forceinline__ float d2_row(const float *v, int q)
+{
+    using C = Coef<float>;
+    const float o = v[4 + q];
+    return C::d2_1 * ((v[5 + q] - o) + (v[3 + q] - o)) - C::d2_2 * ((v[6 + q] - o) + (v[2 + q] - o)) +
+           C::d2_3 * ((v[7 + q] - o) + (v[1 + q] - o)) - C::d2_4 * ((v[8 + q] - o) + (v[q] - o));
+}
+
+// The same along z from 9 vectors f(iz - 4 .. iz + 4) of 4 columns.
+__device__ __forceinline__ float d2_col(const float4 *v, int q)
+{
+    using C = Coef<float>;
+    const float o = comp(v[4], q);
+    return C::d2_1 * ((comp(v[5], q) - o) + (comp(v[3], q) - o)) -
+           C::d2_2 * ((comp(v[6], q) - o) + (comp(v[2], q) - o)) +
+           C::d2_3 * ((comp(v[7], q) - o) + (comp(v[1], q) - o)) -
+           C::d2_4 * ((comp(v[8], q) - o) + (comp(v[0], q) - o));
+}
+
+// Max over the warp, one atomic per warp (values are >= 0).
+__device__ __forceinline__ void warp_max_to(float v, float *dst)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > 0.f) atomicMax((unsigned *)dst, __float_as_uint(v));
+}
+
+template <typename S> struct Vec4Store;
+template <> struct Vec4Store<float> {
+    static __device__ __forceinline__ void put(float *p, const float (&v)[4])
+    {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+
+// ------------------------------------------------------------------ forward tiles
+
+// Per-shot scalars of a forward step, gathered once per block.
+struct FwdShot {
+    long so;        // shot offset in the per-shot arrays
+    long rec_base;  // record index of column 0 at this step (receivers at rec_base + ix)
+    long img;       // image offset, in elements of the store type
+    int sx, sz, rz, rx0, rx1, pad;
+    float w, sc;    // wavelet sample, image scale
+};
+
+template <int ST, bool EXACT>
+__global__ void __launch_bounds__(kTmaThreads, 4)
+k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, int cur, int img_slot, int sg)
+{
+    using Cd = Codec<float, ST>;
+    extern __shared__ __align__(128) unsigned char dsm_raw[];
+    FwdStage *stage = reinterpret_cast<FwdStage *>(aligned_dsm(dsm_raw));
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int act[kMaxGroup];
+    __shared__ FwdShot ps[kMaxGroup];
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
+    const DevShot gsh = b.shots[blockIdx.z * sg];  // every shot of the group has this window
+    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch;
+    if (x0 > nx - 5 || z0 > nz - 5) return;  // no interior point in this tile
+    const int na = active_shots(b, sg, act, false, g, ntb);
+    if (na == 0) return;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
+    if (tid < na) {
+        const int s = act[tid];
+        const DevShot sh = b.shots[s];
+        const int it = g - (ntb - sh.nt);
+        FwdShot q;
+        q.so = (long)s * b.slot;
+        q.rec_base = sh.rec_off + (long)it * (sh.rx1 - sh.rx0) - sh.rx0;
+        q.img = ((long)s * b.n_img + (img_slot >= 0 ? img_slot : 0)) * 2 * b.slot;
+        q.sx = sh.sx; q.sz = sh.sz; q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.pad = 0;
+        q.w = b.wavelet[it];
+        q.sc = 1.f;
+        if (img_slot >= 0 && Cd::scaled) {
+            q.sc = image_scale(b.amax[(long)s * (b.nt_max + 1) + g], (float)b.inv_dh2);
+            if (blockIdx.x == 0 && blockIdx.y == 0) b.scale[(long)s * b.nt_max + g] = q.sc;
+        }
+        ps[tid] = q;
+    }
+    __syncthreads();
+    auto issue = [&](int a) {
+        const int s = act[a];
+        FwdStage &S = stage[a & 1];
+        uint64_t *br = &bar[a & 1];
+        mbar_expect_tx(br, (unsigned)sizeof(FwdStage));
+        tma_load_3d(S.P, &maps.lvl[cur], br, x0 - kRad, z0 - kRad, s);
+        tma_load_3d(S.F, &maps.lvl[2 + cur], br, x0 - kRad, z0 - kRad, s);
+        tma_load_3d(S.Pv, &maps.inc[0], br, x0, z0, s);
+        tma_load_3d(S.Fv, &maps.inc[1], br, x0, z0, s);
+    };
+    if (tid == 0) {
+        issue(0);
+        if (na > 1) issue(1);
+    }
+    const int c4 = 4 * (tid & 7), r = tid >> 3;
+    const int ix0 = x0 + c4, iz = z0 + r;
+    const int cpml = b.cpml;
+    bool m[4], L[4];  // points finished here, layer points (stencils to scratch)
+    bool any = false, all = true, anyL = false;
+    float mh[4], mp[4], mn[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int ix = ix0 + q;
+        const bool in = ix < nx && iz < nz && interior(ix, iz, nx, nz);
+        L[q] = in && layer_point(ix, iz, nx, nz, cpml);
+        m[q] = in && !L[q];
+        any |= m[q];
+        all &= m[q];
+        anyL |= L[q];
+        const long mi = (long)iz * b.mpitch + gsh.x0 + ix;
+        mh[q] = m[q] ? b.mh[mi] : 0.f;
+        mp[q] = m[q] ? b.mp[mi] : 0.f;
+        mn[q] = m[q] ? b.mn[mi] : 0.f;
+    }
+    const long ipt = (long)iz * pitch + ix0;
+    float *const Pn0 = b.lvl[1 - cur], *const Fn0 = b.lvl[3 - cur];
+    float *const Pv0 = b.lvl[4], *const Fv0 = b.lvl[5];
+    for (int a = 0; a < na; a++) {
+        if (!stage_ready(&bar[a & 1], (a >> 1) & 1, b.status)) {
+            if (a + 1 < na) drain_stage(&bar[(a + 1) & 1], ((a + 1) >> 1) & 1);
+            return;
+        }
+        const FwdStage &S = stage[a & 1];
+        const FwdShot &sh = ps[a];
+        const long so = sh.so;
+        float lmax = 0.f;
+        if (any || anyL) {
+            float pv[12];
+            {
+                const float *row = &S.P[r + kRad][c4];
+                const float4 a0 = ld4(row), a1 = ld4(row + 4), a2 = ld4(row + 8);
+                pv[0] = a0.x; pv[1] = a0.y; pv[2] = a0.z; pv[3] = a0.w;
+                pv[4] = a1.x; pv[5] = a1.y; pv[6] = a1.z; pv[7] = a1.w;
+                pv[8] = a2.x; pv[9] = a2.y; pv[10] = a2.z; pv[11] = a2.w;
+            }
+            float4 fz[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) fz[k] = ld4(&S.F[r + k][c4 + kRad]);
+            const float4 vP = ld4(&S.Pv[r][c4]), vF = ld4(&S.Fv[r][c4]);
+            const float w = sh.w;
+            const bool src_row = iz == sh.sz;
+            float nP[4], nF[4], iP[4], iF[4], gG[4], gH[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float G = d2_row(pv, q) * b.inv_dh2;
+                const float H = d2_col(fz, q) * b.inv_dh2;
+                const float mpH = mp[q] * H;
+                float vp = comp(vP, q) + (mh[q] * G + mpH);
+                float vf = comp(vF, q) + (mn[q] * G + mpH);
+                if (src_row && ix0 + q == sh.sx) { vp += w; vf += w; }
+                iP[q] = vp;
+                iF[q] = vf;
+                nP[q] = pv[4 + q] + vp;
+                nF[q] = comp(fz[4], q) + vf;
+                gG[q] = G;
+                gH[q] = H;
+                if (Cd::scaled && m[q]) lmax = fmaxf(lmax, fmaxf(fabsf(nP[q]), fabsf(nF[q])));
+            }
+            if (anyL) {  // Dxx P, Dzz F of the layer points, for k_fwd_cpml
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (L[q]) {
+                        b.scr[0][so + ipt + q] = gG[q];
+                        b.scr[1][so + ipt + q] = gH[q];
+                    }
+            }
+            float *Pn = Pn0 + so, *Fn = Fn0 + so, *Pv = Pv0 + so, *Fv = Fv0 + so;
+            if (all) {
+                Vec4Store<float>::put(Pv + ipt, iP);
+                Vec4Store<float>::put(Fv + ipt, iF);
+                Vec4Store<float>::put(Pn + ipt, nP);
+                Vec4Store<float>::put(Fn + ipt, nF);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (m[q]) {
+                        Pv[ipt + q] = iP[q];
+                        Fv[ipt + q] = iF[q];
+                        Pn[ipt + q] = nP[q];
+                        Fn[ipt + q] = nF[q];
+                    }
+            }
+            if (iz == sh.rz) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int ix = ix0 + q;
+                    if (m[q] && ix >= sh.rx0 && ix < sh.rx1) b.rec[sh.rec_base + ix] = nP[q] + nF[q];
+                }
+            }
+            if (img_slot >= 0) {
+                typename Cd::S *img = (typename Cd::S *)b.store + sh.img;
+                const float sc = sh.sc;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (m[q]) {
+                        img[ipt + q] = Cd::enc(gG[q], sc, b.status);
+                        img[b.slot + ipt + q] = Cd::enc(gH[q], sc, b.status);
+                    }
+            }
+        }
+        if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)act[a] * (b.nt_max + 1) + g + 1]);
+        __syncthreads();  // every thread is done with this stage
+        if (tid == 0 && a + 2 < na) {
+            fence_proxy_async();
+            issue(a + 2);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ adjoint tiles
+
+// Per-shot scalars of an adjoint step, gathered once per block.
+struct AdjShot {
+    long so;        // shot offset in the per-shot arrays
+    long res_base;  // residual index of column 0 at this step (residual at res_base + ix)
+    long img;       // image offset in elements of the store type, < 0: no image this step
+    int rz, rx0, rx1, zimg;  // receiver row and columns, image plane for the TMA load
+    float inv_sc;   // inverse image scale
+};
+
+template <int ST, bool EXACT>
+__global__ void __launch_bounds__(kTmaThreads, 3)
+k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int img_base, int sg)
+{
+    using Cd = Codec<float, ST>;
+    using Stage = AdjStage<typename Cd::S>;
+    extern __shared__ __align__(128) unsigned char dsm_raw[];
+    unsigned char *dsm = aligned_dsm(dsm_raw);
+    Stage *stage = reinterpret_cast<Stage *>(dsm);
+    float(*MH)[TH] = reinterpret_cast<float(*)[TH]>(dsm + 2 * sizeof(Stage));  // [TT][TH]
+    float(*MN)[TH] = MH + TT;                                                  // [TT][TH]
+    float(*MP)[TT] = reinterpret_cast<float(*)[TT]>(MN + TT);                  // [TH][TT]
+    float(*U)[TH] = reinterpret_cast<float(*)[TH]>(MP + TH);                   // [TT][TH]
+    float(*V)[TT] = reinterpret_cast<float(*)[TT]>(U + TT);                    // [TH][TT]
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int act[kMaxGroup];
+    __shared__ AdjShot ps[kMaxGroup];
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
+    const int grp = blockIdx.z;
+    const DevShot gsh = b.shots[grp * sg];
+    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch;
+    if (x0 > nx - 5 || z0 > nz - 5) return;  // no interior point in this tile
+    const int na = active_shots(b, sg, act, true, j, ntb);
+    if (na == 0) return;
+    const int lag = EXACT ? 0 : 1;
+    const int img_g = ntb - 1 - lag - j;  // global step of the image this iteration needs
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
+    if (tid < na) {
+        const int s = act[tid];
+        const DevShot sh = b.shots[s];
+        const int mm = sh.nt - j;
+        AdjShot q;
+        q.so = (long)s * b.slot;
+        q.res_base = sh.rec_off + (long)(mm - 1) * (sh.rx1 - sh.rx0) - sh.rx0;
+        const bool im = mm - 1 - lag >= 0;
+        q.zimg = (int)(((long)s * b.n_img + (img_g - img_base)) * 2);
+        q.img = im ? (long)q.zimg * b.slot : -1;
+        q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1;
+        q.inv_sc = (im && Cd::scaled) ? 1.f / b.scale[(long)s * b.nt_max + img_g] : 1.f;
+        ps[tid] = q;
+    }
+    __syncthreads();
+    auto issue = [&](int a) {
+        const int s = act[a];
+        Stage &S = stage[a & 1];
+        uint64_t *br = &bar[a & 1];
+        const bool im = ps[a].img >= 0;
+        mbar_expect_tx(br, (unsigned)(im ? sizeof(Stage) : sizeof(Stage) - sizeof(S.I)));
+        tma_load_3d(S.P, &maps.lvl[cur], br, x0 - kRad, z0 - kRad, s);
+        tma_load_3d(S.F, &maps.lvl[2 + cur], br, x0 - kRad, z0 - kRad, s);
+        tma_load_3d(S.Pw, &maps.inc[0], br, x0, z0, s);
+        tma_load_3d(S.Fw, &maps.inc[1], br, x0, z0, s);
+        if (im) tma_load_3d(S.I, &maps.img, br, x0, z0, ps[a].zimg);
+    };
+    if (tid == 0) {
+        issue(0);
+        if (na > 1) issue(1);
+    }
+    // model tiles of the group's window: v_hor, v_nmo with the x-halo, v_po with the z-halo
+    for (int k = tid; k < TT * TH; k += kTmaThreads) {
+        const int rr = k / TH, cc = k - rr * TH;
+        const int gx = x0 - kRad + cc, gz = z0 + rr;
+        const bool in = gx >= 0 && gx < nx && gz < nz;
+        const long mi = (long)gz * b.mpitch + gsh.x0 + gx;
+        MH[rr][cc] = in ? b.mh[mi] : 0.f;
+        MN[rr][cc] = in ? b.mn[mi] : 0.f;
+    }
+    for (int k = tid; k < TH * TT; k += kTmaThreads) {
+        const int rr = k / TT, cc = k - rr * TT;
+        const int gx = x0 + cc, gz = z0 - kRad + rr;
+        const bool in = gx < nx && gz >= 0 && gz < nz;
+        MP[rr][cc] = in ? b.mp[(long)gz * b.mpitch + gsh.x0 + gx] : 0.f;
+    }
+    const int cpml = b.cpml;
+    const int aw = EXACT ? cpml + kRad : cpml;
+    const int c4 = 4 * (tid & 7), r = tid >> 3;
+    const int ix0 = x0 + c4, iz = z0 + r;
+    bool m[4], L[4];  // points finished here, points the layers touch (stencils to scratch)
+    bool any = false, all = true, anyL = false;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int ix = ix0 + q;
+        const bool in = ix < nx && iz < nz && interior(ix, iz, nx, nz);
+        L[q] = in && layer_point(ix, iz, nx, nz, aw);
+        m[q] = in && !L[q];
+        any |= m[q];
+        all &= m[q];
+        anyL |= L[q];
+    }
+    const long ipt = (long)iz * pitch + ix0;
+    float *const lPn0 = b.lvl[1 - cur], *const lFn0 = b.lvl[3 - cur];
+    float *const lPw0 = b.lvl[4], *const lFw0 = b.lvl[5];
+    float ah[4] = {0.f, 0.f, 0.f, 0.f}, ap[4] = {0.f, 0.f, 0.f, 0.f}, an[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int a = 0; a < na; a++) {
+        if (!stage_ready(&bar[a & 1], (a >> 1) & 1, b.status)) {
+            if (a + 1 < na) drain_stage(&bar[(a + 1) & 1], ((a + 1) >> 1) & 1);
+            return;
+        }
+        const Stage &S = stage[a & 1];
+        // U = dt^2 (v_hor lP + v_nmo lF) on the x-halo tile, V = dt^2 v_po (lP + lF) on the z-halo tile
+        for (int k = tid; k < TT * (TH / 4); k += kTmaThreads) {
+            const int rr = k / (TH / 4), cc = 4 * (k - rr * (TH / 4));
+            const float4 p = ld4(&S.P[rr + kRad][cc]), f = ld4(&S.F[rr + kRad][cc]);
+            const float4 h = ld4(&MH[rr][cc]), n = ld4(&MN[rr][cc]);
+            *reinterpret_cast<float4 *>(&U[rr][cc]) =
+                make_float4(h.x * p.x + n.x * f.x, h.y * p.y + n.y * f.y, h.z * p.z + n.z * f.z, h.w * p.w + n.w * f.w);
+        }
+        for (int k = tid; k < TH * (TT / 4); k += kTmaThreads) {
+            const int rr = k / (TT / 4), cc = 4 * (k - rr * (TT / 4));
+            const float4 p = ld4(&S.P[rr][cc + kRad]), f = ld4(&S.F[rr][cc + kRad]), v = ld4(&MP[rr][cc]);
+            *reinterpret_cast<float4 *>(&V[rr][cc]) =
+                make_float4(v.x * (p.x + f.x), v.y * (p.y + f.y), v.z * (p.z + f.z), v.w * (p.w + f.w));
+        }
+        __syncthreads();
+        const AdjShot &sh = ps[a];
+        const long so = sh.so;
+        if (anyL) {
+            // stencil values of the layer points for k_adj_cpml
+            if (EXACT) {
+                float uv[12];
+                const float4 a0 = ld4(&U[r][c4]), a1 = ld4(&U[r][c4 + 4]), a2 = ld4(&U[r][c4 + 8]);
+                uv[0] = a0.x; uv[1] = a0.y; uv[2] = a0.z; uv[3] = a0.w;
+                uv[4] = a1.x; uv[5] = a1.y; uv[6] = a1.z; uv[7] = a1.w;
+                uv[8] = a2.x; uv[9] = a2.y; uv[10] = a2.z; uv[11] = a2.w;
+                float4 vz[9];
+#pragma unroll
+                for (int k = 0; k < 9; k++) vz[k] = ld4(&V[r + k][c4]);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (L[q]) {
+                        b.scr[0][so + ipt + q] = d2_row(uv, q) * b.inv_dh2;
+                        b.scr[1][so + ipt + q] = d2_col(vz, q) * b.inv_dh2;
+                    }
+            } else {
+                // the reference keeps the four second derivatives of the model-weighted
+                // fields apart (src/parallelcalls.cu:200-214); its zeta recursion needs them
+                using C = Coef<float>;
+                const float c2[5] = {C::d2_0, C::d2_1, -C::d2_2, C::d2_3, -C::d2_4};
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (!L[q]) continue;
+                    const int c = c4 + q;
+                    float p2cx = 0.f, r2dx = 0.f, p2cz = 0.f, r2cz = 0.f;
+#pragma unroll
+                    for (int k = -4; k <= 4; k++) {
+                        const float w2 = c2[k < 0 ? -k : k];
+                        p2cx += w2 * (MH[r][c + kRad + k] * S.P[r + kRad][c + kRad + k]);
+                        r2dx += w2 * (MN[r][c + kRad + k] * S.F[r + kRad][c + kRad + k]);
+                        p2cz += w2 * (MP[r + kRad + k][c] * S.P[r + kRad + k][c + kRad]);
+                        r2cz += w2 * (MP[r + kRad + k][c] * S.F[r + kRad + k][c + kRad]);
+                    }
+                    b.scr[0][so + ipt + q] = p2cx * b.inv_dh2;
+                    b.scr[1][so + ipt + q] = r2dx * b.inv_dh2;
+                    b.scr[2][so + ipt + q] = p2cz * b.inv_dh2;
+                    b.scr[3][so + ipt + q] = r2cz * b.inv_dh2;
+                }
+            }
+        }
+        if (any) {
+            float uv[12];
+            {
+                const float4 a0 = ld4(&U[r][c4]), a1 = ld4(&U[r][c4 + 4]), a2 = ld4(&U[r][c4 + 8]);
+                uv[0] = a0.x; uv[1] = a0.y; uv[2] = a0.z; uv[3] = a0.w;
+                uv[4] = a1.x; uv[5] = a1.y; uv[6] = a1.z; uv[7] = a1.w;
+                uv[8] = a2.x; uv[9] = a2.y; uv[10] = a2.z; uv[11] = a2.w;
+            }
+            float4 vz[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) vz[k] = ld4(&V[r + k][c4]);
+            const float4 wP = ld4(&S.Pw[r][c4]), wF = ld4(&S.Fw[r][c4]);
+            const float4 cP = ld4(&S.P[r + kRad][c4 + kRad]), cF = ld4(&S.F[r + kRad][c4 + kRad]);
+            const bool rec_row = iz == sh.rz;
+            float nwP[4], nwF[4], nP[4], nF[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                float wp = comp(wP, q) + d2_row(uv, q) * b.inv_dh2;
+                float wf = comp(wF, q) + d2_col(vz, q) * b.inv_dh2;
+                const int ix = ix0 + q;
+                if (rec_row && m[q] && ix >= sh.rx0 && ix < sh.rx1) {
+                    const float d = b.rec[sh.res_base + ix];
+                    wp += d;
+                    wf += d;
+                }
+                nwP[q] = wp;
+                nwF[q] = wf;
+                nP[q] = comp(cP, q) + wp;
+                nF[q] = comp(cF, q) + wf;
+            }
+            float *lPn = lPn0 + so, *lFn = lFn0 + so, *lPw = lPw0 + so, *lFw = lFw0 + so;
+            if (all) {
+                Vec4Store<float>::put(lPw + ipt, nwP);
+                Vec4Store<float>::put(lFw + ipt, nwF);
+                Vec4Store<float>::put(lPn + ipt, nP);
+                Vec4Store<float>::put(lFn + ipt, nF);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (m[q]) {
+                        lPw[ipt + q] = nwP[q];
+                        lFw[ipt + q] = nwF[q];
+                        lPn[ipt + q] = nP[q];
+                        lFn[ipt + q] = nF[q];
+                    }
+            }
+            if (sh.img >= 0) {
+                const float inv_sc = sh.inv_sc;
+                const float kk = b.img_scale;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float Gv = Cd::dec(S.I[0][r][c4 + q], inv_sc), Hv = Cd::dec(S.I[1][r][c4 + q], inv_sc);
+                    ah[q] += kk * Gv * nP[q];
+                    ap[q] += kk * Hv * (nP[q] + nF[q]);
+                    an[q] += kk * Gv * nF[q];
+                }
+            }
+        }
+        __syncthreads();  // stage, U and V are free again
+        if (tid == 0 && a + 2 < na) {
+            fence_proxy_async();
+            issue(a + 2);
+        }
+    }
+    if (!any) return;
+    // one read-modify-write per group: g[grp] += the group's imaging
+    const long gi = (long)grp * b.slot + ipt;
+    float *g0 = b.g[0] + gi, *g1 = b.g[1] + gi, *g2 = b.g[2] + gi;
+    if (all) {  // no layer point in a full vector group
+        const float4 o0 = ld4(g0), o1 = ld4(g1), o2 = ld4(g2);
+        *reinterpret_cast<float4 *>(g0) = make_float4(o0.x + ah[0], o0.y + ah[1], o0.z + ah[2], o0.w + ah[3]);
+        *reinterpret_cast<float4 *>(g1) = make_float4(o1.x + ap[0], o1.y + ap[1], o1.z + ap[2], o1.w + ap[3]);
+        *reinterpret_cast<float4 *>(g2) = make_float4(o2.x + an[0], o2.y + an[1], o2.z + an[2], o2.w + an[3]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (m[q]) {
+                g0[q] += ah[q];
+                g1[q] += ap[q];
+                g2[q] += an[q];
+            }
+    }
+}
+
+// ------------------------------------------------------------------ layer points
+
+// Forward, points inside the layers (after k_fwd_strip and k_fwd_tma): the
+// zeta recursion and the memory-variable derivatives of
+// src/parallelcalls.cu:55-84 on the stencil values k_fwd_tma left in
+// scr[0] (Dxx P) and scr[1] (Dzz F), then the update, source, receivers,
+// image and state max.  Derivatives of psi_x are taken only within 4
+// columns of a side layer and those of psi_z only within 4 rows of the
+// bottom one: elsewhere every term is exactly zero.
+template <int ST, bool EXACT>
+__global__ void __launch_bounds__(kStripBlock) k_fwd_cpml(Batch<float> b, int g, int ntb, int cur, int img_slot)
+{
+    using Cd = Codec<float, ST>;
+    const int s = blockIdx.y;
+    const DevShot sh = b.shots[s];
+    const int it = g - (ntb - sh.nt);
+    if (it < 0) return;
+    const int nx = sh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
+    const StripMap smap = StripMap::make(nx, nz, cpml);
+    const long so = (long)s * b.slot;
+    const float *P = b.lvl[cur] + so, *F = b.lvl[2 + cur] + so;
+    float *Pn = b.lvl[1 - cur] + so, *Fn = b.lvl[3 - cur] + so;
+    float *Pv = b.lvl[4] + so, *Fv = b.lvl[5] + so;
+    const float *psx = b.cp[0] + so, *psz = b.cp[1] + so;
+    float *zx = b.cp[2] + so, *zz = b.cp[3] + so;
+    const float *p2s = b.scr[0] + so, *r2s = b.scr[1] + so;
+    float sc = 1.f;
+    typename Cd::S *img = nullptr;
+    if (img_slot >= 0) {
+        img = (typename Cd::S *)b.store + ((long)s * b.n_img + img_slot) * 2 * b.slot;
+        if (Cd::scaled) sc = image_scale(b.amax[(long)s * (b.nt_max + 1) + g], (float)b.inv_dh2);
+    }
+    const float w = b.wavelet[it];
+    const int nrec = sh.rx1 - sh.rx0;
+    float lmax = 0.f;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < smap.count();
+         k += (long)gridDim.x * blockDim.x) {
+        int ix, iz;
+        smap.point(k, ix, iz);
+        const long i = (long)iz * pitch + ix;
+        const float p2 = p2s[i], r2 = r2s[i];
+        float G = p2, H = r2;
+        {
+            const bool xl = ix < cpml || ix > nx - cpml - 1;
+            const float tx = (ix < cpml + kRad || ix > nx - cpml - 1 - kRad) ? d1_strided(psx, i, 1) * b.inv_dh : 0.f;
+            const float zxn = xl ? coef_x(b.cpb, ix, nx, cpml) * zx[i] + coef_x(b.cpa, ix, nx, cpml) * (p2 + tx) : 0.f;
+            if (xl) zx[i] = zxn;
+            G = p2 + (tx + zxn);
+        }
+        {
+            const bool zl = iz > nz - cpml - 1;
+            const float tz = iz > nz - cpml - 1 - kRad ? d1_strided(psz, i, pitch) * b.inv_dh : 0.f;
+            const float zzn = zl ? coef_z(b.cpb, iz, nz, cpml) * zz[i] + coef_z(b.cpa, iz, nz, cpml) * (r2 + tz) : 0.f;
+            if (zl) zz[i] = zzn;
+            H = r2 + (tz + zzn);
+        }
+        const long mi = (long)iz * b.mpitch + sh.x0 + ix;
+        const float mpH = b.mp[mi] * H;
+        float vp = Pv[i] + (b.mh[mi] * G + mpH);
+        float vf = Fv[i] + (b.mn[mi] * G + mpH);
+        if (ix == sh.sx && iz == sh.sz) { vp += w; vf += w; }
+        Pv[i] = vp;
+        Fv[i] = vf;
+        const float pn = P[i] + vp, fn = F[i] + vf;
+        Pn[i] = pn;
+        Fn[i] = fn;
+        if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1) b.rec[sh.rec_off + (long)it * nrec + (ix - sh.rx0)] = pn + fn;
+        if (img) {
+            img[i] = Cd::enc(EXACT ? G : p2, sc, b.status);
+            img[b.slot + i] = Cd::enc(EXACT ? H : r2, sc, b.status);
+        }
+        if (Cd::scaled) lmax = fmaxf(lmax, fmaxf(fabsf(pn), fabsf(fn)));
+    }
+    if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)s * (b.nt_max + 1) + g + 1]);
+}
+
+// Adjoint, the points k_adj_tma left (after the strip pass and k_adj_tma).
+// One thread per point loops over the active shots of its group in order
+// and adds their imaging to the group's gradient in one read-modify-write.
+//  EXACT: points within 4 of a layer, + Dxx(S ax Zx') - Dx(S ax Yx') (and the
+//         same along z) on scr[0] = Dxx U, scr[1] = Dzz V.
+//  reference: points inside the layers, the zeta recursion of
+//         src/parallelcalls.cu:216-243 on scr[0..3] = p2cx, r2dx, p2cz, r2cz.
+template <int ST, bool EXACT>
+__global__ void __launch_bounds__(kStripBlock) k_adj_cpml(Batch<float> b, int j, int ntb, int cur, int zsel,
+                                                          int img_base, int sg)
+{
+    using Cd = Codec<float, ST>;
+    const int grp = blockIdx.y;
+    const int s0 = grp * sg, s1 = min(s0 + sg, b.B);
+    const DevShot gsh = b.shots[s0];
+    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
+    const StripMap smap = StripMap::make(nx, nz, EXACT ? cpml + kRad : cpml);
+    const int lag = EXACT ? 0 : 1;
+    const int img_g = ntb - 1 - lag - j;
+    using C = Coef<float>;
+    const float c2[5] = {C::d2_0, C::d2_1, -C::d2_2, C::d2_3, -C::d2_4};
+    const float c1[4] = {C::d1_1, -C::d1_2, C::d1_3, -C::d1_4};
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < smap.count();
+         k += (long)gridDim.x * blockDim.x) {
+        int ix, iz;
+        smap.point(k, ix, iz);
+        const long i = (long)iz * pitch + ix;
+        const bool xl = ix < cpml || ix > nx - cpml - 1, zl = iz > nz - cpml - 1;
+        const bool xn = ix < cpml + kRad || ix > nx - cpml - 1 - kRad, zn = iz > nz - cpml - 1 - kRad;
+        const float ax = coef_x(b.cpa, ix, nx, cpml), bx = coef_x(b.cpb, ix, nx, cpml);
+        const float az = coef_z(b.cpa, iz, nz, cpml), bz = coef_z(b.cpb, iz, nz, cpml);
+        float ah = 0.f, ap = 0.f, an = 0.f;
+        bool touched = false;
+        for (int s = s0; s < s1; s++) {
+            const DevShot sh = b.shots[s];
+            if (j >= sh.nt) continue;
+            touched = true;
+            const long so = (long)s * b.slot;
+            float ex, ez;
+            if (EXACT) {
+                ex = b.scr[0][so + i];
+                ez = b.scr[1][so + i];
+                if (xn) {
+                    const float *Zx = b.cp[3 - zsel] + so, *Yx = b.cp[0] + so;
+                    float a2 = c2[0] * ax * Zx[i], a1 = 0.f;
+#pragma unroll
+                    for (int q = 1; q <= 4; q++) {
+                        const float aP = coef_x(b.cpa, ix + q, nx, cpml), aM = coef_x(b.cpa, ix - q, nx, cpml);
+                        a2 += c2[q] * (aP * Zx[i + q] + aM * Zx[i - q]);
+                        a1 += c1[q - 1] * (aP * Yx[i + q] - aM * Yx[i - q]);
+                    }
+                    ex += a2 * b.inv_dh2 - a1 * b.inv_dh;
+                }
+                if (zn) {
+                    const float *Zz = b.cp[5 - zsel] + so, *Yz = b.cp[1] + so;
+                    float a2 = c2[0] * az * Zz[i], a1 = 0.f;
+#pragma unroll
+                    for (int q = 1; q <= 4; q++) {
+                        const long up = i + (long)q * pitch, dn = i - (long)q * pitch;
+                        const float aP = coef_z(b.cpa, iz + q, nz, cpml), aM = coef_z(b.cpa, iz - q, nz, cpml);
+                        a2 += c2[q] * (aP * Zz[up] + aM * Zz[dn]);
+                        a1 += c1[q - 1] * (aP * Yz[up] - aM * Yz[dn]);
+                    }
+                    ez += a2 * b.inv_dh2 - a1 * b.inv_dh;
+                }
+            } else {
+                const float p2cx = b.scr[0][so + i], r2dx = b.scr[1][so + i];
+                const float p2cz = b.scr[2][so + i], r2cz = b.scr[3][so + i];
+                const float *psixcx = b.cp[0] + so, *psixcz = b.cp[1] + so;
+                const float *psizdx = b.cp[2] + so, *psizcz = b.cp[3] + so;
+                float *zxcx = b.cp[4] + so, *zxcz = b.cp[5] + so, *zzdx = b.cp[6] + so, *zzcz = b.cp[7] + so;
+                float dxcx = 0.f, dzdx = 0.f, dxcz = 0.f, dzcz = 0.f;
+                if (xn) {
+                    dxcx = d1_strided(psixcx, i, 1) * b.inv_dh;
+                    dzdx = d1_strided(psizdx, i, 1) * b.inv_dh;
+                }
+                if (zn) {
+                    dxcz = d1_strided(psixcz, i, pitch) * b.inv_dh;
+                    dzcz = d1_strided(psizcz, i, pitch) * b.inv_dh;
+                }
+                float n1 = 0.f, n2 = 0.f, n3 = 0.f, n4 = 0.f;
+                if (xl) {
+                    n1 = bx * zxcx[i] + ax * (dxcx + p2cx);
+                    n3 = bx * zzdx[i] + ax * (dzdx + r2dx);
+                    zxcx[i] = n1;
+                    zzdx[i] = n3;
+                }
+                if (zl) {
+                    n2 = bz * zxcz[i] + az * (dxcz + p2cz);
+                    n4 = bz * zzcz[i] + az * (dzcz + r2cz);
+                    zxcz[i] = n2;
+                    zzcz[i] = n4;
+                }
+                ex = (p2cx + r2dx) + ((n1 + dxcx) + (n3 + dzdx));
+                ez = (p2cz + r2cz) + ((n2 + dxcz) + (n4 + dzcz));
+            }
+            const float *lP = b.lvl[cur] + so, *lF = b.lvl[2 + cur] + so;
+            float *lPw = b.lvl[4] + so, *lFw = b.lvl[5] + so;
+            float wp = lPw[i] + ex, wf = lFw[i] + ez;
+            const int mm = sh.nt - j;
+            if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1) {
+                const float d = b.rec[sh.rec_off + (long)(mm - 1) * (sh.rx1 - sh.rx0) + (ix - sh.rx0)];
+                wp += d;
+                wf += d;
+            }
+            lPw[i] = wp;
+            lFw[i] = wf;
+            const float pn = lP[i] + wp, fn = lF[i] + wf;
+            b.lvl[1 - cur][so + i] = pn;
+            b.lvl[3 - cur][so + i] = fn;
+            if (mm - 1 - lag >= 0) {
+                const typename Cd::S *img =
+                    (const typename Cd::S *)b.store + ((long)s * b.n_img + (img_g - img_base)) * 2 * b.slot;
+                const float inv_sc = Cd::scaled ? 1.f / b.scale[(long)s * b.nt_max + img_g] : 1.f;
+                const float kk = b.img_scale;
+                const float Gv = Cd::dec(img[i], inv_sc), Hv = Cd::dec(img[b.slot + i], inv_sc);
+                ah += kk * Gv * pn;
+                ap += kk * Hv * (pn + fn);
+                an += kk * Gv * fn;
+            }
+        }
+        if (touched) {
+            const long gi = (long)grp * b.slot + i;
+            b.g[0][gi] += ah;
+            b.g[1][gi] += ap;
+            b.g[2][gi] += an;
+        }
+    }
+}
+
+inline size_t fwd_tma_smem() { return 128 + 2 * sizeof(FwdStage); }
+template <typename S> inline size_t adj_tma_smem()
+{
+    return 128 + 2 * sizeof(AdjStage<S>) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
+}
+
+}  // namespace fwi

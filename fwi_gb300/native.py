@@ -53,6 +53,12 @@ class Config(C.Structure):
                 ("device", C.c_int)]
 
 
+class InvertOpts(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("lbfgs_m", C.c_int), ("first_alpha", C.c_float * 3),
+                ("alpha0", C.c_float), ("max_halvings", C.c_int), ("reset_alpha", C.c_int),
+                ("flag_min", C.c_int), ("flag_max", C.c_int)]
+
+
 class Shot(C.Structure):
     _fields_ = [("sx", C.c_int), ("sz", C.c_int), ("rz", C.c_int), ("rx0", C.c_int),
                 ("rx1", C.c_int), ("nt", C.c_int), ("x0", C.c_int), ("nxw", C.c_int)]
@@ -104,6 +110,9 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_last_launches", [_p], _l)
         _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
         _sig(L, "fwi_residual_misfit_noalloc", [_p, _p, _p, _p, _l, _i, _p, _p])
+        _sig(L, "fwi_invert_defaults", [C.POINTER(InvertOpts)], None)
+        _sig(L, "fwi_invert", [_p, shotp, _i, _p, _p, C.POINTER(InvertOpts), _p, C.POINTER(_i)])
+        _sig(L, "fwi_set_frequency", [_p, _f, _i])
         # reference-compatible ABI: float* device pointers, ints, floats
         _sig(L, "pre_variables_h", [_p] * 6 + [_i, _i], None)
         _sig(L, "CPML_x_h", [_p, _p, _i, _f, _i, _f, _f, _f, _f, _f], None)
@@ -249,6 +258,25 @@ class Context:
         w = np.ascontiguousarray(w, self.dtype) if isinstance(w, np.ndarray) else w
         _checked(w, self.dtype, len(w), "wavelet")
         _check(lib().fwi_set_wavelet(self._h, ptr(w), len(w)), "fwi_set_wavelet")
+
+    def set_frequency(self, f, nt):
+        _check(lib().fwi_set_frequency(self._h, float(f), int(nt)), "fwi_set_frequency")
+
+    def invert(self, shots, obs, mask=None, **opts):
+        """One band of the reference's inversion loop in the C driver; returns the misfits."""
+        o = InvertOpts()
+        lib().fwi_invert_defaults(C.byref(o))
+        for k, v in opts.items():
+            if k == "first_alpha":
+                o.first_alpha[:] = list(v)
+            else:
+                setattr(o, k, v)
+        self._inputs(shots, obs, mask)
+        hist = np.zeros(o.iterations, np.float64)
+        done = C.c_int(0)
+        _check(lib().fwi_invert(self._h, shots, len(shots), ptr(obs), ptr(mask), C.byref(o),
+                                hist.ctypes.data, C.byref(done)), "fwi_invert")
+        return hist[: done.value]
 
     def set_ricker(self, f, nt):
         _check(lib().fwi_set_ricker(self._h, float(f), int(nt)), "fwi_set_ricker")

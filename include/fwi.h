@@ -156,6 +156,31 @@ int fwi_lbfgs_update(void *ctx, float alpha_v, float alpha_d, float alpha_e, int
 /* Model back to m_back (src/main.c:777-784). */
 int fwi_restore_model(void *ctx);
 
+/* ---- host driver (C) ----
+ * One frequency band of the reference's inversion loop (src/main.c:396-801) over the calls
+ * above: steepest first step, then L-BFGS directions with the backtracking line search
+ * (halve alpha on a NaN misfit or one above the iteration's; more than max_halvings
+ * halvings restore the model and end the band).  misfit_history (optional) receives the
+ * misfit of each iteration's gradient. */
+typedef struct {
+    int iterations;       /* src/main.c:12: 100 */
+    int lbfgs_m;          /* src/main.c:59: 5 */
+    float first_alpha[3]; /* steepest-descent lengths for v_hor, v_po, v_nmo (src/main.c:567) */
+    float alpha0;         /* first L-BFGS step length (src/main.c:62: 1) */
+    int max_halvings;     /* src/main.c:777: 5 */
+    int reset_alpha;      /* 0: alpha and the halving count persist over the band, as the reference */
+    int flag_min, flag_max; /* clamps of update_LBFGS (src/parallelcalls.cu:343-404) */
+} fwi_invert_opts;
+
+void fwi_invert_defaults(fwi_invert_opts *opts);
+int fwi_invert(void *ctx, const fwi_shot *shots, int nshots, const void *obs,
+               const unsigned char *mask, const fwi_invert_opts *opts, double *misfit_history,
+               int *iterations_done);
+
+/* Next frequency band (src/main.c:318-319, 328-333, 802): CPML profiles for peak
+ * frequency f and a Ricker wavelet of nt samples at f. */
+int fwi_set_frequency(void *ctx, float f, int nt);
+
 /* Chain rule to the Vp / epsilon / delta parameterisation of the current model:
  * dJ/dVp = 2 Vp (g_po + (1 + 2 eps) g_hor + (1 + 2 delta) g_nmo),
  * dJ/deps = 2 Vp^2 g_hor, dJ/ddelta = 2 Vp^2 g_nmo (outputs [nz][nx]). */
