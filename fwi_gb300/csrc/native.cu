@@ -2,9 +2,11 @@
 //
 // One context = one device, one stream, one arena of device memory.  A
 // gradient call runs the shots in batches of up to max_shots:
-//   forward (2 launches / step, images kept per the storage mode)
+//   forward (FP32: strip pass, layer tiles and layer points on a side stream
+//   beside the interior tiles, 4 launches / step; FP64: 2), images kept per
+//   the storage mode
 //   -> residual + FP64 misfit partials
-//   -> adjoint + imaging (2 launches / step)
+//   -> adjoint + imaging (4 launches / step in FP32, 2 in FP64)
 //   -> deterministic reduction of the per-shot gradients into the model grid.
 // The L-BFGS update of src/main.c:539-800 runs on the device with FP64 dot
 // products reduced by the last block to finish (no host round trip).
@@ -18,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -60,8 +63,8 @@ int make_tensor_map_3d(CUtensorMap *map, const void *base, CUtensorMapDataType t
 // compiled into this unit).
 struct HostTmaMaps {
     CUtensorMap lvl[4];
-    CUtensorMap inc[2];
-    CUtensorMap img;
+    CUtensorMap px[2];
+    CUtensorMap fz[2];
 };
 
 }  // namespace fwi
@@ -464,6 +467,7 @@ template <typename T> struct Ctx : CtxBase {
     long slot = 0, mslot = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[4] = {};
+    fwi::StepStreams ss{};  // st, plus the side stream of the FP32 strip passes
     std::vector<void *> allocs;
     // model and setup
     T *vh = nullptr, *vp = nullptr, *vn = nullptr, *mh = nullptr, *mp = nullptr, *mn = nullptr;
@@ -502,8 +506,14 @@ template <typename T> struct Ctx : CtxBase {
     {
         if (st) cudaStreamSynchronize(st);
         for (void *p : allocs) cudaFree(p);
+        if (ss.side) cudaStreamSynchronize(ss.side);
+        if (ss.strip) cudaStreamSynchronize(ss.strip);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : {ss.fork, ss.join, ss.strip_done})
+            if (e) cudaEventDestroy(e);
+        if (ss.side) cudaStreamDestroy(ss.side);
+        if (ss.strip) cudaStreamDestroy(ss.strip);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -540,14 +550,28 @@ template <typename T> struct Ctx : CtxBase {
         TRY(cudaSetDevice(cfg.device));
         TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         for (auto &e : ev) TRY(cudaEventCreate(&e));
+        ss.main = st;
+        if (sizeof(T) == 4) {
+            // the side stream carries the step's critical path (strip pass -> layer
+            // tiles -> layer points): the highest priority, so that its blocks take
+            // SM slots ahead of the interior tiles' as those free up
+            int lo = 0, hi = 0;
+            TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            TRY(cudaStreamCreateWithPriority(&ss.side, cudaStreamNonBlocking, hi));
+            TRY(cudaStreamCreateWithPriority(&ss.strip, cudaStreamNonBlocking, hi));
+            TRY(cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming));
+            TRY(cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming));
+            TRY(cudaEventCreateWithFlags(&ss.strip_done, cudaEventDisableTiming));
+        }
         for (T **p : {&vh, &vp, &vn, &mh, &mp, &mn}) TRY(alloc(p, mslot));
         TRY(alloc(&cpa, cfg.cpml + 1));
         TRY(alloc(&cpb, cfg.cpml + 1));
         TRY(alloc(&wavelet, nt_max));
         for (auto &p : lvl) TRY(alloc(&p, (size_t)B * slot));
+        if (sizeof(T) == 4)
+            for (auto &p : scr) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : cp) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : gs) TRY(alloc(&p, (size_t)B * slot));
-        for (auto &p : scr) TRY(alloc(&p, (size_t)B * slot));
         if (cfg.store == FWI_STORE_CHECKPOINT) {
             ck_every = checkpoint_interval(cfg);
             n_ck = (nt_max + ck_every - 1) / ck_every;
@@ -601,29 +625,35 @@ template <typename T> struct Ctx : CtxBase {
             int rc = make_tensor_map_3d(&m.lvl[k], lv[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 40, 40, 1);
             if (rc) return rc;
         }
-        for (int k = 0; k < 2; k++) {
-            int rc = make_tensor_map_3d(&m.inc[k], lv[4 + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 32, 32, 1);
+        for (int k = 0; k < 2; k++) {  // P levels with the x-halo only, F levels with the z-halo only
+            int rc = make_tensor_map_3d(&m.px[k], lv[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 40, 32, 1);
+            if (rc) return rc;
+            rc = make_tensor_map_3d(&m.fz[k], lv[2 + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 32, 40, 1);
             if (rc) return rc;
         }
-        const int st_t = store_type();
-        const CUtensorMapDataType it = st_t == kStoreHalf ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                       : st_t == kStoreBf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
-                                                            : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-        return make_tensor_map_3d(&m.img, store, it, (int)store_elem(), pitch, nz, (long)B * n_img * 2, 32, 32, 2);
+        return FWI_OK;
     }
 
-    // Shots per group for a batch: groups need identical windows; with them,
-    // enough groups to give about four blocks per SM.
+    // Shots per group for a batch: groups need identical windows.  The tile
+    // passes are latency-bound, so many short blocks beat few long ones: the
+    // group count gives about three waves of adjoint tile blocks (3 resident
+    // per SM of a 152-SM GB300).  Measured on 601 x 301, 32 shots: 5 shots
+    // per group (7 groups) 56.8 shots/s, 8: 53.8, 3: 52.3, 16: 40.6.
     int shots_per_group(const std::vector<DevShot> &bs, int nxm) const
     {
         if (!use_tma) return 1;
         for (const DevShot &d : bs)
             if (d.x0 != bs[0].x0 || d.nx != bs[0].nx) return 1;
-        const long tiles = (long)((nxm + 31) / 32) * ((nz + 31) / 32);
-        const int nb = (int)bs.size();
-        long groups = std::max<long>(1, std::min<long>(nb, (4L * 152 + tiles - 1) / tiles));
-        int sg = (int)((nb + groups - 1) / groups);
-        return std::max(1, std::min(sg, 64));
+        if (const char *e = getenv("FWI_SHOTS_PER_GROUP")) {  // tuning override
+            const int v = atoi(e);
+            if (v >= 1) return std::min(v, 64);
+        }
+        const long tiles = (long)((nxm - 5) / 32 + 1) * ((nz - 5) / 32 + 1);  // tiles holding interior points
+        const long slots = 3L * 152;
+        const long nb = (long)bs.size();
+        const long groups = std::max(1L, std::min(nb, (3 * slots + tiles / 2) / tiles));
+        const long sg = (nb + groups - 1) / groups;
+        return (int)std::max(1L, std::min(sg, 64L));
     }
 
     // CPML table by distance (src/main.c:48-51: L = CPML dh, d0 = -3 ln R / (2 L), in T)
@@ -753,9 +783,9 @@ template <typename T> struct Ctx : CtxBase {
         b.B = nb; b.nz = nz; b.pitch = pitch; b.mpitch = mpitch; b.cpml = cfg.cpml; b.nt_max = nt_max;
         b.slot = slot;
         for (int k = 0; k < 6; k++) b.lvl[k] = lvl[k];
+        for (int k = 0; k < 4; k++) b.scr[k] = scr[k];
         for (int k = 0; k < 8; k++) b.cp[k] = cp[k];
         for (int k = 0; k < 3; k++) b.g[k] = gs[k];
-        for (int k = 0; k < 4; k++) b.scr[k] = scr[k];
         b.store = store; b.store_type = store_type(); b.n_img = n_img;
         b.scale = scale; b.amax = amax; b.rec = rec; b.shots = shots;
         b.mh = mh; b.mp = mp; b.mn = mn; b.cpa = cpa; b.cpb = cpb; b.wavelet = wavelet;
@@ -810,6 +840,7 @@ template <typename T> struct Ctx : CtxBase {
         if (rc) return rc;
         TRY(cudaEventRecord(ev[0], st));
         long launches0 = launches;
+        const long kps = sizeof(T) == 4 ? 4 : 2;  // kernels per time step (see the file comment)
         if (want_grad)
             for (auto &p : grad) TRY(cudaMemsetAsync(p, 0, mslot * sizeof(T), st));
         TRY(cudaMemsetAsync(misfit, 0, sizeof(double), st));
@@ -849,11 +880,11 @@ template <typename T> struct Ctx : CtxBase {
                     int rc2 = save_checkpoint(g / ck_every, nb, cur);
                     if (rc2) return rc2;
                 }
-                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt) ? g : -1, exact, st);
+                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt) ? g : -1, exact, ss);
                 cur ^= 1;
             }
             TRY_LAUNCH();
-            launches += 2L * ntb;
+            launches += kps * ntb;
             TRY(cudaEventRecord(e1, st));
             if (obs_in) {
                 k_residual<T><<<dim3(kRedBlocks, nb), kRedThreads, 0, st>>>(rec, obs, mask_in ? mask : nullptr, shots,
@@ -872,12 +903,12 @@ template <typename T> struct Ctx : CtxBase {
                 int zsel = 0;
                 if (!ckpt) {
                     for (int j = 0; j < ntb; j++) {
-                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, st);
+                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, ss);
                         cur ^= 1;
                         zsel ^= 1;
                     }
                     TRY_LAUNCH();
-                    launches += 2L * ntb;
+                    launches += kps * ntb;
                 } else {
                     // segments from the last: recompute its images from the checkpoint, then
                     // run the adjoint iterations that image inside it
@@ -897,22 +928,22 @@ template <typename T> struct Ctx : CtxBase {
                         int rc2 = restore_checkpoint(seg, nb, rcur);
                         if (rc2) return rc2;
                         for (int g = a; g < e; g++) {
-                            fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, g - a, exact, st);
+                            fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, g - a, exact, ss);
                             rcur ^= 1;
                         }
-                        launches += 2L * (e - a);
+                        launches += kps * (e - a);
                         for (; j < ntb && ntb - 1 - lag - j >= a; j++) {
-                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a, st);
+                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a, ss);
                             cur ^= 1;
                             zsel ^= 1;
-                            launches += 2;
+                            launches += kps;
                         }
                     }
                     for (; j < ntb; j++) {  // iterations without an image (reference lag)
-                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, st);
+                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, ss);
                         cur ^= 1;
                         zsel ^= 1;
-                        launches += 2;
+                        launches += kps;
                     }
                     TRY_LAUNCH();
                 }
@@ -1163,7 +1194,7 @@ size_t fwi_config_bytes(const fwi_config *c)
     const long nrec = c->max_receivers > 0 ? c->max_receivers : win;
     size_t b = 0;
     b += (size_t)(6 + 3 + 12) * mslot * e;                 // models, gradient, L-BFGS work arrays
-    b += (size_t)c->max_shots * slot * e * (6 + 8 + 3 + 4); // levels, CPML state, gradients, scratch
+    b += (size_t)c->max_shots * slot * e * (6 + 8 + 3 + (e == 4 ? 4 : 0));  // levels, CPML state, gradients, FP32 scratch
     if (c->store == FWI_STORE_CHECKPOINT) {
         const long k = checkpoint_interval(*c), n = (c->nt_max + k - 1) / k;
         b += (size_t)c->max_shots * slot * e * (8 * n + 10); // checkpoints, recompute state

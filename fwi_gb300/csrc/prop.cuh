@@ -519,8 +519,9 @@ inline void fwd_dispatch(const Batch<T> &b, int nx_max, int g, int ntb, int cur,
 
 template <typename T>
 void launch_forward_step(const Batch<T> &b, int nx_max, int g, int ntb, int cur, int img_slot,
-                         bool exact, cudaStream_t st)
+                         bool exact, const StepStreams &ss)
 {
+    cudaStream_t st = ss.main;
     k_fwd_strip<T><<<strip_grid(b, nx_max), kStripBlock, 0, st>>>(b, g, ntb, cur);
     switch (b.store_type) {
     case kStoreHalf: fwd_dispatch<T, kStoreHalf>(b, nx_max, g, ntb, cur, img_slot, exact, st); break;
@@ -541,8 +542,9 @@ inline void adj_dispatch(const Batch<T> &b, int nx_max, int j, int ntb, int cur,
 
 template <typename T>
 void launch_adjoint_step(const Batch<T> &b, int nx_max, int j, int ntb, int cur, int zsel,
-                         bool exact, int img_base, cudaStream_t st)
+                         bool exact, int img_base, const StepStreams &ss)
 {
+    cudaStream_t st = ss.main;
     if (exact) k_adj_strip_exact<T><<<strip_grid(b, nx_max), kStripBlock, 0, st>>>(b, j, cur, zsel);
     else k_adj_strip_ref<T><<<strip_grid(b, nx_max), kStripBlock, 0, st>>>(b, j, cur);
     switch (b.store_type) {

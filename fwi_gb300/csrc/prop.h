@@ -24,9 +24,9 @@ template <typename T> struct Batch {
     int B, nz, pitch, mpitch, cpml, nt_max;
     long slot;
     T *lvl[6];      // P level 0, P level 1, F level 0, F level 1, P increment, F increment
+    T *scr[4];      // per-shot scratch: stencil values of layer points, layer tiles -> layer kernels
     T *cp[8];       // CPML memory variables (forward uses 0..3)
     T *g[3];        // per-shot gradient accumulators: v_hor, v_po, v_nmo
-    T *scr[4];      // per-shot scratch: stencil values the tile kernels hand to the layer kernels
     void *store;    // images: [B][n_img][2][slot] of the store type
     int store_type; // StoreType
     int n_img;      // image slots per shot
@@ -56,13 +56,23 @@ template <typename T> struct Batch {
 // reference's leapfrog; in FP32 it keeps the low bits of each small update
 // that 2 u^n - u^{n-1} + dt^2 (...) rounds away.
 
+// Streams of a step.  The FP32 path runs the interior tiles on `main`, the
+// layer tiles on `side` and the strip pass (CPML memory variables) on
+// `strip`, all three from the current time level; the layer points follow on
+// `side` once the strip pass is done, and `main` joins `side` before the next
+// step.  side == nullptr: everything on `main` (as the FP64 path does).
+struct StepStreams {
+    cudaStream_t main = nullptr, side = nullptr, strip = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, strip_done = nullptr;
+};
+
 // Forward global step g.  `cur` is the level holding each shot's current
 // state; the new state goes to level 1 - cur.  With img_slot >= 0 the
 // step's images go to that slot (G, H for exact imaging, Dxx P and Dzz F for
 // the reference's).  Receiver traces are always recorded.
 template <typename T>
 void launch_forward_step(const Batch<T> &b, int nx_max, int g, int ntb, int cur, int img_slot,
-                         bool exact, cudaStream_t st);
+                         bool exact, const StepStreams &ss);
 
 // Adjoint iteration j: lambda^m, m = nt_s - j, of every shot with nt_s > j.
 // `cur` holds lambda^{m+1}; lambda^m goes to level 1 - cur (increment form).  `zsel`
@@ -71,6 +81,6 @@ void launch_forward_step(const Batch<T> &b, int nx_max, int g, int ntb, int cur,
 // (that step - img_base); img_base <= that step is the caller's contract.
 template <typename T>
 void launch_adjoint_step(const Batch<T> &b, int nx_max, int j, int ntb, int cur, int zsel,
-                         bool exact, int img_base, cudaStream_t st);
+                         bool exact, int img_base, const StepStreams &ss);
 
 }  // namespace fwi

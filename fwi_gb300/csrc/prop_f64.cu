@@ -2,6 +2,7 @@
 #include "prop.cuh"
 
 namespace fwi {
-template void launch_forward_step<double>(const Batch<double> &, int, int, int, int, int, bool, cudaStream_t);
-template void launch_adjoint_step<double>(const Batch<double> &, int, int, int, int, int, bool, int, cudaStream_t);
+template void launch_forward_step<double>(const Batch<double> &, int, int, int, int, int, bool, const StepStreams &);
+template void launch_adjoint_step<double>(const Batch<double> &, int, int, int, int, int, bool, int,
+                                           const StepStreams &);
 }  // namespace fwi

@@ -1,21 +1,22 @@
 // FP32 main passes (sm_103a): TMA tile loads, shot groups, 4-wide vectors.
 //
-// Per time step:
-//  * tile kernels (k_fwd_tma, k_adj_tma): one block per 32x32 tile loops over
-//    a group of shots that share a window; each shot's tiles (the two stencil
-//    fields with a 4-point halo, the increments, the images) arrive by
-//    cp.async.bulk.tensor into one of two shared-memory stages while the
-//    block computes the previous shot (2-stage mbarrier pipeline, one issuing
-//    thread).  A thread owns 4 consecutive points of a row: the x-stencil is 3
-//    ld.shared.v4, the z-stencil 9, stores are 16-byte vectors.  Points the
-//    CPML layers do not touch are finished here; for the others the block
-//    only writes the stencil values it already has to per-shot scratch.  The
-//    adjoint sums the imaging of its group in registers (one gradient
-//    read-modify-write per group and step).
-//  * layer kernels (k_fwd_cpml, k_adj_cpml): the points inside the layers
-//    (forward, reference adjoint) or within 4 points of them (exact adjoint,
-//    whose transpose terms reach that far): memory-variable terms, update,
-//    receivers and imaging, from the scratch stencil values.
+// A 32 x 32 tile block loops over a group of shots that share a window.  Each
+// shot's halo'd fields arrive by cp.async.bulk.tensor into one of kStages
+// shared-memory stages while the block computes earlier shots (mbarrier
+// pipeline, one issuing thread); the increments and images, read at each
+// thread's own 4 points, are loaded into registers before the stage wait.  A
+// thread owns 4 consecutive points of a row: the x-stencil is 3
+// ld.shared.v4, the z-stencil 9, stores are 16-byte vectors.  The adjoint
+// sums the imaging of its group in registers (one gradient read-modify-write
+// per group and step).
+//
+// The tiles split in two launches of the same kernel template:
+//  * interior tiles (LAYER = false): no point the CPML layers touch;
+//  * layer tiles (LAYER = true): the CPML terms of their layer points too,
+//    from the memory variables the strip pass of the step has advanced.
+// Both read only the current time level and write disjoint points, so the
+// host runs [strip pass -> layer tiles] on a side stream concurrently with
+// the interior tiles.
 #pragma once
 
 #include "prop.cuh"
@@ -31,31 +32,41 @@ constexpr int kMaxGroup = 64;
 // Tensor maps over one batch's per-shot arrays ([B][nz][pitch]) and images.
 struct TmaMaps {
     CUtensorMap lvl[4];  // P level 0/1, F level 0/1: 40 x 40 boxes
-    CUtensorMap inc[2];  // P and F increments: 32 x 32 boxes
-    CUtensorMap img;     // images [B * n_img * 2][nz][pitch]: 32 x 32 x 2 boxes
+    CUtensorMap px[2];   // P level 0/1: 40 x 32 boxes (x-halo)
+    CUtensorMap fz[2];   // F level 0/1: 32 x 40 boxes (z-halo)
 };
 
+// The forward operator takes Dxx of P and Dzz of F only: each is staged
+// with the halo along its own axis.
+// Only the fields read with a halo are staged; the increments and images,
+// read at each thread's own 4 points, are loaded straight into registers.
 struct FwdStage {
-    float P[TH][TH];
-    float F[TH][TH];
-    float Pv[TT][TT];
-    float Fv[TT][TT];
+    float P[TT][TH];
+    float F[TH][TT];
 };
 
-template <typename S> struct AdjStage {
+struct AdjStage {
     float P[TH][TH];
     float F[TH][TH];
-    float Pw[TT][TT];
-    float Fw[TT][TT];
-    S I[2][TT][TT];
 };
 
-// Points the layers touch: those are left to the point-list kernels.  `aw`
-// is the CPML width (forward, reference adjoint) or CPML width + 4 (exact
-// adjoint).  Same shape as the reference's strip predicate.
+constexpr int kStages = 3;  // TMA pipeline depth over a group's shots
+
+// Points the layers touch.  `aw` is the CPML width (forward, reference
+// adjoint) or CPML width + 4 (exact adjoint, whose transpose terms reach 4
+// points further).  Same shape as the reference's strip predicate.
 __device__ __forceinline__ bool layer_point(int ix, int iz, int nx, int nz, int aw)
 {
     return ix < aw || ix > nx - aw - 1 || iz > nz - aw - 1;
+}
+
+// Role of the tile at (x0, z0): 0 no interior point, 1 interior tile (no
+// layer point), 2 layer tile.
+__device__ __forceinline__ int tile_role(int x0, int z0, int nx, int nz, int aw)
+{
+    if (x0 > nx - 5 || z0 > nz - 5) return 0;
+    const int xa = max(x0, 4), xb = min(x0 + TT - 1, nx - 5), zb = min(z0 + TT - 1, nz - 5);
+    return (xa < aw || xb > nx - aw - 1 || zb > nz - aw - 1) ? 2 : 1;
 }
 
 __device__ __forceinline__ unsigned char *aligned_dsm(unsigned char *p)
@@ -84,11 +95,13 @@ __device__ __forceinline__ bool stage_ready(uint64_t *bar, unsigned parity, unsi
     return true;
 }
 
-// After a failed wait: give the loads still in flight a bounded time to land
-// before the block's shared memory is released.
-__device__ __forceinline__ void drain_stage(uint64_t *bar, unsigned parity)
+// After a failed wait at shot a: give the loads still in flight (shots a + 1
+// .. a + kStages - 1) a bounded time to land before the block's shared memory
+// is released.
+__device__ __forceinline__ void drain_stages(uint64_t *bar, int a, int na)
 {
-    if (threadIdx.x == 0) (void)mbar_wait(bar, parity);
+    if (threadIdx.x == 0)
+        for (int k = a + 1; k < min(a + kStages, na); k++) (void)mbar_wait(&bar[k % kStages], (k / kStages) & 1);
     __syncthreads();
 }
 
@@ -142,7 +155,32 @@ template <> struct Vec4Store<float> {
     {
         *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
     }
+    static __device__ __forceinline__ void get(const float *p, float (&v)[4])
+    {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
 };
+// 16-bit image values: 4 per 8-byte access (callers keep p 8-byte aligned).
+template <typename H> struct Vec4Store16 {
+    static __device__ __forceinline__ void put(H *p, const H (&v)[4])
+    {
+        uint2 u;
+        u.x = (uint32_t)__builtin_bit_cast(uint16_t, v[0]) | ((uint32_t)__builtin_bit_cast(uint16_t, v[1]) << 16);
+        u.y = (uint32_t)__builtin_bit_cast(uint16_t, v[2]) | ((uint32_t)__builtin_bit_cast(uint16_t, v[3]) << 16);
+        *reinterpret_cast<uint2 *>(p) = u;
+    }
+    static __device__ __forceinline__ void get(const H *p, H (&v)[4])
+    {
+        const uint2 u = *reinterpret_cast<const uint2 *>(p);
+        v[0] = __builtin_bit_cast(H, (uint16_t)(u.x & 0xffffu));
+        v[1] = __builtin_bit_cast(H, (uint16_t)(u.x >> 16));
+        v[2] = __builtin_bit_cast(H, (uint16_t)(u.y & 0xffffu));
+        v[3] = __builtin_bit_cast(H, (uint16_t)(u.y >> 16));
+    }
+};
+template <> struct Vec4Store<__half> : Vec4Store16<__half> {};
+template <> struct Vec4Store<__nv_bfloat16> : Vec4Store16<__nv_bfloat16> {};
 
 // ------------------------------------------------------------------ forward tiles
 
@@ -155,26 +193,25 @@ struct FwdShot {
     float w, sc;    // wavelet sample, image scale
 };
 
-template <int ST, bool EXACT>
+template <int ST, bool EXACT, bool LAYER>  // EXACT: unused (see the launcher)
 __global__ void __launch_bounds__(kTmaThreads, 4)
 k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, int cur, int img_slot, int sg)
 {
     using Cd = Codec<float, ST>;
     extern __shared__ __align__(128) unsigned char dsm_raw[];
     FwdStage *stage = reinterpret_cast<FwdStage *>(aligned_dsm(dsm_raw));
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[kStages];
     __shared__ int act[kMaxGroup];
     __shared__ FwdShot ps[kMaxGroup];
     const int tid = threadIdx.x;
     const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
     const DevShot gsh = b.shots[blockIdx.z * sg];  // every shot of the group has this window
-    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch;
-    if (x0 > nx - 5 || z0 > nz - 5) return;  // no interior point in this tile
+    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
+    if (tile_role(x0, z0, nx, nz, cpml) != (LAYER ? 2 : 1)) return;
     const int na = active_shots(b, sg, act, false, g, ntb);
     if (na == 0) return;
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int k = 0; k < kStages; k++) mbar_init(&bar[k], 1);
         mbar_init_fence();
     }
     if (tid < na) {
@@ -190,36 +227,31 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
         q.sc = 1.f;
         if (img_slot >= 0 && Cd::scaled) {
             q.sc = image_scale(b.amax[(long)s * (b.nt_max + 1) + g], (float)b.inv_dh2);
-            if (blockIdx.x == 0 && blockIdx.y == 0) b.scale[(long)s * b.nt_max + g] = q.sc;
+            if (blockIdx.x == 0 && blockIdx.y == 0) b.scale[(long)s * b.nt_max + g] = q.sc;  // a layer tile
         }
         ps[tid] = q;
     }
     __syncthreads();
     auto issue = [&](int a) {
         const int s = act[a];
-        FwdStage &S = stage[a & 1];
-        uint64_t *br = &bar[a & 1];
+        FwdStage &S = stage[a % kStages];
+        uint64_t *br = &bar[a % kStages];
         mbar_expect_tx(br, (unsigned)sizeof(FwdStage));
-        tma_load_3d(S.P, &maps.lvl[cur], br, x0 - kRad, z0 - kRad, s);
-        tma_load_3d(S.F, &maps.lvl[2 + cur], br, x0 - kRad, z0 - kRad, s);
-        tma_load_3d(S.Pv, &maps.inc[0], br, x0, z0, s);
-        tma_load_3d(S.Fv, &maps.inc[1], br, x0, z0, s);
+        tma_load_3d(S.P, &maps.px[cur], br, x0 - kRad, z0, s);
+        tma_load_3d(S.F, &maps.fz[cur], br, x0, z0 - kRad, s);
     };
-    if (tid == 0) {
-        issue(0);
-        if (na > 1) issue(1);
-    }
+    if (tid == 0)
+        for (int k = 0; k < min(kStages, na); k++) issue(k);
     const int c4 = 4 * (tid & 7), r = tid >> 3;
     const int ix0 = x0 + c4, iz = z0 + r;
-    const int cpml = b.cpml;
-    bool m[4], L[4];  // points finished here, layer points (stencils to scratch)
+    bool m[4], L[4];  // points finished here, layer points (layer tiles: stencils to scratch)
     bool any = false, all = true, anyL = false;
     float mh[4], mp[4], mn[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int ix = ix0 + q;
         const bool in = ix < nx && iz < nz && interior(ix, iz, nx, nz);
-        L[q] = in && layer_point(ix, iz, nx, nz, cpml);
+        L[q] = LAYER && in && layer_point(ix, iz, nx, nz, cpml);
         m[q] = in && !L[q];
         any |= m[q];
         all &= m[q];
@@ -233,18 +265,23 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     float *const Pn0 = b.lvl[1 - cur], *const Fn0 = b.lvl[3 - cur];
     float *const Pv0 = b.lvl[4], *const Fv0 = b.lvl[5];
     for (int a = 0; a < na; a++) {
-        if (!stage_ready(&bar[a & 1], (a >> 1) & 1, b.status)) {
-            if (a + 1 < na) drain_stage(&bar[(a + 1) & 1], ((a + 1) >> 1) & 1);
-            return;
-        }
-        const FwdStage &S = stage[a & 1];
         const FwdShot &sh = ps[a];
         const long so = sh.so;
+        float4 vP = make_float4(0.f, 0.f, 0.f, 0.f), vF = vP;
+        if (any) {  // own points only: issued before the wait, in flight during it
+            vP = ld4(Pv0 + so + ipt);
+            vF = ld4(Fv0 + so + ipt);
+        }
+        if (!stage_ready(&bar[a % kStages], (a / kStages) & 1, b.status)) {
+            drain_stages(bar, a, na);
+            return;
+        }
+        const FwdStage &S = stage[a % kStages];
         float lmax = 0.f;
         if (any || anyL) {
             float pv[12];
             {
-                const float *row = &S.P[r + kRad][c4];
+                const float *row = &S.P[r][c4];
                 const float4 a0 = ld4(row), a1 = ld4(row + 4), a2 = ld4(row + 8);
                 pv[0] = a0.x; pv[1] = a0.y; pv[2] = a0.z; pv[3] = a0.w;
                 pv[4] = a1.x; pv[5] = a1.y; pv[6] = a1.z; pv[7] = a1.w;
@@ -252,15 +289,27 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
             }
             float4 fz[9];
 #pragma unroll
-            for (int k = 0; k < 9; k++) fz[k] = ld4(&S.F[r + k][c4 + kRad]);
-            const float4 vP = ld4(&S.Pv[r][c4]), vF = ld4(&S.Fv[r][c4]);
+            for (int k = 0; k < 9; k++) fz[k] = ld4(&S.F[r + k][c4]);
             const float w = sh.w;
             const bool src_row = iz == sh.sz;
-            float nP[4], nF[4], iP[4], iF[4], gG[4], gH[4];
+            float gG[4], gH[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                const float G = d2_row(pv, q) * b.inv_dh2;
-                const float H = d2_col(fz, q) * b.inv_dh2;
+                gG[q] = d2_row(pv, q) * b.inv_dh2;
+                gH[q] = d2_col(fz, q) * b.inv_dh2;
+            }
+            if (LAYER && anyL) {  // Dxx P, Dzz F of the layer points, for k_fwd_cpml
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (L[q]) {
+                        b.scr[0][so + ipt + q] = gG[q];
+                        b.scr[1][so + ipt + q] = gH[q];
+                    }
+            }
+            float nP[4], nF[4], iP[4], iF[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float G = gG[q], H = gH[q];
                 const float mpH = mp[q] * H;
                 float vp = comp(vP, q) + (mh[q] * G + mpH);
                 float vf = comp(vF, q) + (mn[q] * G + mpH);
@@ -269,17 +318,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
                 iF[q] = vf;
                 nP[q] = pv[4 + q] + vp;
                 nF[q] = comp(fz[4], q) + vf;
-                gG[q] = G;
-                gH[q] = H;
                 if (Cd::scaled && m[q]) lmax = fmaxf(lmax, fmaxf(fabsf(nP[q]), fabsf(nF[q])));
-            }
-            if (anyL) {  // Dxx P, Dzz F of the layer points, for k_fwd_cpml
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (L[q]) {
-                        b.scr[0][so + ipt + q] = gG[q];
-                        b.scr[1][so + ipt + q] = gH[q];
-                    }
             }
             float *Pn = Pn0 + so, *Fn = Fn0 + so, *Pv = Pv0 + so, *Fv = Fv0 + so;
             if (all) {
@@ -305,66 +344,110 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
                 }
             }
             if (img_slot >= 0) {
-                typename Cd::S *img = (typename Cd::S *)b.store + sh.img;
+                using SI = typename Cd::S;
+                SI *img = (SI *)b.store + sh.img;
                 const float sc = sh.sc;
+                SI eG[4], eH[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (m[q]) {
-                        img[ipt + q] = Cd::enc(gG[q], sc, b.status);
-                        img[b.slot + ipt + q] = Cd::enc(gH[q], sc, b.status);
-                    }
+                for (int q = 0; q < 4; q++) {
+                    eG[q] = Cd::enc(m[q] ? gG[q] : 0.f, sc, b.status);
+                    eH[q] = Cd::enc(m[q] ? gH[q] : 0.f, sc, b.status);
+                }
+                if (all) {
+                    Vec4Store<SI>::put(img + ipt, eG);
+                    Vec4Store<SI>::put(img + b.slot + ipt, eH);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (m[q]) {
+                            img[ipt + q] = eG[q];
+                            img[b.slot + ipt + q] = eH[q];
+                        }
+                }
             }
         }
         if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)act[a] * (b.nt_max + 1) + g + 1]);
         __syncthreads();  // every thread is done with this stage
-        if (tid == 0 && a + 2 < na) {
+        if (tid == 0 && a + kStages < na) {
             fence_proxy_async();
-            issue(a + 2);
+            issue(a + kStages);
         }
     }
 }
 
 // ------------------------------------------------------------------ adjoint tiles
 
+// Reference adjoint, layer point: the four second derivatives of the
+// model-weighted fields (src/parallelcalls.cu:200-214), kept apart because
+// the zeta recursion needs them, from the tile's staged fields and model
+// tiles to scratch (k_adj_cpml reads them).  (c, r): column and row in the tile.
+struct Scr4 {
+    float *p[4];
+    float inv_dh2;
+};
+
+__device__ __noinline__ void ref_layer_stencils(const Scr4 &o, long i, int c, int r, const float (*MH)[TH],
+                                                const float (*MN)[TH], const float (*MP)[TT], const float (*P)[TH],
+                                                const float (*F)[TH])
+{
+    using C = Coef<float>;
+    const float c2[5] = {C::d2_0, C::d2_1, -C::d2_2, C::d2_3, -C::d2_4};
+    float p2cx = 0.f, r2dx = 0.f, p2cz = 0.f, r2cz = 0.f;
+#pragma unroll
+    for (int k = -4; k <= 4; k++) {
+        const float w2 = c2[k < 0 ? -k : k];
+        p2cx += w2 * (MH[r][c + kRad + k] * P[r + kRad][c + kRad + k]);
+        r2dx += w2 * (MN[r][c + kRad + k] * F[r + kRad][c + kRad + k]);
+        p2cz += w2 * (MP[r + kRad + k][c] * P[r + kRad + k][c + kRad]);
+        r2cz += w2 * (MP[r + kRad + k][c] * F[r + kRad + k][c + kRad]);
+    }
+    o.p[0][i] = p2cx * o.inv_dh2;
+    o.p[1][i] = r2dx * o.inv_dh2;
+    o.p[2][i] = p2cz * o.inv_dh2;
+    o.p[3][i] = r2cz * o.inv_dh2;
+}
+
 // Per-shot scalars of an adjoint step, gathered once per block.
 struct AdjShot {
     long so;        // shot offset in the per-shot arrays
     long res_base;  // residual index of column 0 at this step (residual at res_base + ix)
     long img;       // image offset in elements of the store type, < 0: no image this step
-    int rz, rx0, rx1, zimg;  // receiver row and columns, image plane for the TMA load
+    int rz, rx0, rx1, pad;  // receiver row and columns
     float inv_sc;   // inverse image scale
 };
 
-template <int ST, bool EXACT>
+template <int ST, bool EXACT, bool LAYER>
 __global__ void __launch_bounds__(kTmaThreads, 3)
-k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int img_base, int sg)
+k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int zsel, int img_base,
+          int sg)
 {
     using Cd = Codec<float, ST>;
-    using Stage = AdjStage<typename Cd::S>;
+    using Stage = AdjStage;
+    using SI = typename Cd::S;
     extern __shared__ __align__(128) unsigned char dsm_raw[];
     unsigned char *dsm = aligned_dsm(dsm_raw);
     Stage *stage = reinterpret_cast<Stage *>(dsm);
-    float(*MH)[TH] = reinterpret_cast<float(*)[TH]>(dsm + 2 * sizeof(Stage));  // [TT][TH]
-    float(*MN)[TH] = MH + TT;                                                  // [TT][TH]
-    float(*MP)[TT] = reinterpret_cast<float(*)[TT]>(MN + TT);                  // [TH][TT]
-    float(*U)[TH] = reinterpret_cast<float(*)[TH]>(MP + TH);                   // [TT][TH]
-    float(*V)[TT] = reinterpret_cast<float(*)[TT]>(U + TT);                    // [TH][TT]
-    __shared__ __align__(8) uint64_t bar[2];
+    float(*MH)[TH] = reinterpret_cast<float(*)[TH]>(dsm + kStages * sizeof(Stage));  // [TT][TH]
+    float(*MN)[TH] = MH + TT;                                                          // [TT][TH]
+    float(*MP)[TT] = reinterpret_cast<float(*)[TT]>(MN + TT);                          // [TH][TT]
+    float(*U)[TH] = reinterpret_cast<float(*)[TH]>(MP + TH);                           // [TT][TH]
+    float(*V)[TT] = reinterpret_cast<float(*)[TT]>(U + TT);                            // [TH][TT]
+    __shared__ __align__(8) uint64_t bar[kStages];
     __shared__ int act[kMaxGroup];
     __shared__ AdjShot ps[kMaxGroup];
     const int tid = threadIdx.x;
     const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
     const int grp = blockIdx.z;
     const DevShot gsh = b.shots[grp * sg];
-    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch;
-    if (x0 > nx - 5 || z0 > nz - 5) return;  // no interior point in this tile
+    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
+    const int aw = EXACT ? cpml + kRad : cpml;
+    if (tile_role(x0, z0, nx, nz, aw) != (LAYER ? 2 : 1)) return;
     const int na = active_shots(b, sg, act, true, j, ntb);
     if (na == 0) return;
     const int lag = EXACT ? 0 : 1;
     const int img_g = ntb - 1 - lag - j;  // global step of the image this iteration needs
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int k = 0; k < kStages; k++) mbar_init(&bar[k], 1);
         mbar_init_fence();
     }
     if (tid < na) {
@@ -375,29 +458,22 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
         q.so = (long)s * b.slot;
         q.res_base = sh.rec_off + (long)(mm - 1) * (sh.rx1 - sh.rx0) - sh.rx0;
         const bool im = mm - 1 - lag >= 0;
-        q.zimg = (int)(((long)s * b.n_img + (img_g - img_base)) * 2);
-        q.img = im ? (long)q.zimg * b.slot : -1;
-        q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1;
+        q.img = im ? ((long)s * b.n_img + (img_g - img_base)) * 2 * b.slot : -1;
+        q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.pad = 0;
         q.inv_sc = (im && Cd::scaled) ? 1.f / b.scale[(long)s * b.nt_max + img_g] : 1.f;
         ps[tid] = q;
     }
     __syncthreads();
     auto issue = [&](int a) {
         const int s = act[a];
-        Stage &S = stage[a & 1];
-        uint64_t *br = &bar[a & 1];
-        const bool im = ps[a].img >= 0;
-        mbar_expect_tx(br, (unsigned)(im ? sizeof(Stage) : sizeof(Stage) - sizeof(S.I)));
+        Stage &S = stage[a % kStages];
+        uint64_t *br = &bar[a % kStages];
+        mbar_expect_tx(br, (unsigned)sizeof(Stage));
         tma_load_3d(S.P, &maps.lvl[cur], br, x0 - kRad, z0 - kRad, s);
         tma_load_3d(S.F, &maps.lvl[2 + cur], br, x0 - kRad, z0 - kRad, s);
-        tma_load_3d(S.Pw, &maps.inc[0], br, x0, z0, s);
-        tma_load_3d(S.Fw, &maps.inc[1], br, x0, z0, s);
-        if (im) tma_load_3d(S.I, &maps.img, br, x0, z0, ps[a].zimg);
     };
-    if (tid == 0) {
-        issue(0);
-        if (na > 1) issue(1);
-    }
+    if (tid == 0)
+        for (int k = 0; k < min(kStages, na); k++) issue(k);
     // model tiles of the group's window: v_hor, v_nmo with the x-halo, v_po with the z-halo
     for (int k = tid; k < TT * TH; k += kTmaThreads) {
         const int rr = k / TH, cc = k - rr * TH;
@@ -413,17 +489,15 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
         const bool in = gx < nx && gz >= 0 && gz < nz;
         MP[rr][cc] = in ? b.mp[(long)gz * b.mpitch + gsh.x0 + gx] : 0.f;
     }
-    const int cpml = b.cpml;
-    const int aw = EXACT ? cpml + kRad : cpml;
     const int c4 = 4 * (tid & 7), r = tid >> 3;
     const int ix0 = x0 + c4, iz = z0 + r;
-    bool m[4], L[4];  // points finished here, points the layers touch (stencils to scratch)
+    bool m[4], L[4];  // points finished here, points the layers touch (layer tiles: stencils to scratch)
     bool any = false, all = true, anyL = false;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int ix = ix0 + q;
         const bool in = ix < nx && iz < nz && interior(ix, iz, nx, nz);
-        L[q] = in && layer_point(ix, iz, nx, nz, aw);
+        L[q] = LAYER && in && layer_point(ix, iz, nx, nz, aw);
         m[q] = in && !L[q];
         any |= m[q];
         all &= m[q];
@@ -434,11 +508,24 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     float *const lPw0 = b.lvl[4], *const lFw0 = b.lvl[5];
     float ah[4] = {0.f, 0.f, 0.f, 0.f}, ap[4] = {0.f, 0.f, 0.f, 0.f}, an[4] = {0.f, 0.f, 0.f, 0.f};
     for (int a = 0; a < na; a++) {
-        if (!stage_ready(&bar[a & 1], (a >> 1) & 1, b.status)) {
-            if (a + 1 < na) drain_stage(&bar[(a + 1) & 1], ((a + 1) >> 1) & 1);
+        // own points' increments and images: issued before the wait, in flight during it
+        float4 wP = make_float4(0.f, 0.f, 0.f, 0.f), wF = wP;
+        SI iG[4], iH[4];
+        if (any) {
+            const long so = ps[a].so;
+            wP = ld4(lPw0 + so + ipt);
+            wF = ld4(lFw0 + so + ipt);
+            if (ps[a].img >= 0) {
+                const SI *img = (const SI *)b.store + ps[a].img;
+                Vec4Store<SI>::get(img + ipt, iG);
+                Vec4Store<SI>::get(img + b.slot + ipt, iH);
+            }
+        }
+        if (!stage_ready(&bar[a % kStages], (a / kStages) & 1, b.status)) {
+            drain_stages(bar, a, na);
             return;
         }
-        const Stage &S = stage[a & 1];
+        const Stage &S = stage[a % kStages];
         // U = dt^2 (v_hor lP + v_nmo lF) on the x-halo tile, V = dt^2 v_po (lP + lF) on the z-halo tile
         for (int k = tid; k < TT * (TH / 4); k += kTmaThreads) {
             const int rr = k / (TH / 4), cc = 4 * (k - rr * (TH / 4));
@@ -456,8 +543,8 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
         __syncthreads();
         const AdjShot &sh = ps[a];
         const long so = sh.so;
-        if (anyL) {
-            // stencil values of the layer points for k_adj_cpml
+        if (LAYER && anyL) {
+            // stencil values of the layer points, for k_adj_cpml
             if (EXACT) {
                 float uv[12];
                 const float4 a0 = ld4(&U[r][c4]), a1 = ld4(&U[r][c4 + 4]), a2 = ld4(&U[r][c4 + 8]);
@@ -474,28 +561,12 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                         b.scr[1][so + ipt + q] = d2_col(vz, q) * b.inv_dh2;
                     }
             } else {
-                // the reference keeps the four second derivatives of the model-weighted
-                // fields apart (src/parallelcalls.cu:200-214); its zeta recursion needs them
-                using C = Coef<float>;
-                const float c2[5] = {C::d2_0, C::d2_1, -C::d2_2, C::d2_3, -C::d2_4};
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if (!L[q]) continue;
-                    const int c = c4 + q;
-                    float p2cx = 0.f, r2dx = 0.f, p2cz = 0.f, r2cz = 0.f;
-#pragma unroll
-                    for (int k = -4; k <= 4; k++) {
-                        const float w2 = c2[k < 0 ? -k : k];
-                        p2cx += w2 * (MH[r][c + kRad + k] * S.P[r + kRad][c + kRad + k]);
-                        r2dx += w2 * (MN[r][c + kRad + k] * S.F[r + kRad][c + kRad + k]);
-                        p2cz += w2 * (MP[r + kRad + k][c] * S.P[r + kRad + k][c + kRad]);
-                        r2cz += w2 * (MP[r + kRad + k][c] * S.F[r + kRad + k][c + kRad]);
-                    }
-                    b.scr[0][so + ipt + q] = p2cx * b.inv_dh2;
-                    b.scr[1][so + ipt + q] = r2dx * b.inv_dh2;
-                    b.scr[2][so + ipt + q] = p2cz * b.inv_dh2;
-                    b.scr[3][so + ipt + q] = r2cz * b.inv_dh2;
-                }
+                Scr4 o;
+                for (int k = 0; k < 4; k++) o.p[k] = b.scr[k];
+                o.inv_dh2 = b.inv_dh2;
+#pragma unroll 1
+                for (int q = 0; q < 4; q++)
+                    if (L[q]) ref_layer_stencils(o, so + ipt + q, c4 + q, r, MH, MN, MP, S.P, S.F);
             }
         }
         if (any) {
@@ -509,14 +580,19 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
             float4 vz[9];
 #pragma unroll
             for (int k = 0; k < 9; k++) vz[k] = ld4(&V[r + k][c4]);
-            const float4 wP = ld4(&S.Pw[r][c4]), wF = ld4(&S.Fw[r][c4]);
             const float4 cP = ld4(&S.P[r + kRad][c4 + kRad]), cF = ld4(&S.F[r + kRad][c4 + kRad]);
+            float e[4][2];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                e[q][0] = d2_row(uv, q) * b.inv_dh2;
+                e[q][1] = d2_col(vz, q) * b.inv_dh2;
+            }
             const bool rec_row = iz == sh.rz;
             float nwP[4], nwF[4], nP[4], nF[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                float wp = comp(wP, q) + d2_row(uv, q) * b.inv_dh2;
-                float wf = comp(wF, q) + d2_col(vz, q) * b.inv_dh2;
+                float wp = comp(wP, q) + e[q][0];
+                float wf = comp(wF, q) + e[q][1];
                 const int ix = ix0 + q;
                 if (rec_row && m[q] && ix >= sh.rx0 && ix < sh.rx1) {
                     const float d = b.rec[sh.res_base + ix];
@@ -549,7 +625,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                 const float kk = b.img_scale;
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const float Gv = Cd::dec(S.I[0][r][c4 + q], inv_sc), Hv = Cd::dec(S.I[1][r][c4 + q], inv_sc);
+                    const float Gv = Cd::dec(iG[q], inv_sc), Hv = Cd::dec(iH[q], inv_sc);
                     ah[q] += kk * Gv * nP[q];
                     ap[q] += kk * Hv * (nP[q] + nF[q]);
                     an[q] += kk * Gv * nF[q];
@@ -557,16 +633,16 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
             }
         }
         __syncthreads();  // stage, U and V are free again
-        if (tid == 0 && a + 2 < na) {
+        if (tid == 0 && a + kStages < na) {
             fence_proxy_async();
-            issue(a + 2);
+            issue(a + kStages);
         }
     }
     if (!any) return;
     // one read-modify-write per group: g[grp] += the group's imaging
     const long gi = (long)grp * b.slot + ipt;
     float *g0 = b.g[0] + gi, *g1 = b.g[1] + gi, *g2 = b.g[2] + gi;
-    if (all) {  // no layer point in a full vector group
+    if (all) {
         const float4 o0 = ld4(g0), o1 = ld4(g1), o2 = ld4(g2);
         *reinterpret_cast<float4 *>(g0) = make_float4(o0.x + ah[0], o0.y + ah[1], o0.z + ah[2], o0.w + ah[3]);
         *reinterpret_cast<float4 *>(g1) = make_float4(o1.x + ap[0], o1.y + ap[1], o1.z + ap[2], o1.w + ap[3]);
@@ -584,9 +660,9 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
 
 // ------------------------------------------------------------------ layer points
 
-// Forward, points inside the layers (after k_fwd_strip and k_fwd_tma): the
-// zeta recursion and the memory-variable derivatives of
-// src/parallelcalls.cu:55-84 on the stencil values k_fwd_tma left in
+// Forward, points inside the layers (after the strip pass and the layer
+// tiles): the zeta recursion and the memory-variable derivatives of
+// src/parallelcalls.cu:55-84 on the stencil values the layer tiles left in
 // scr[0] (Dxx P) and scr[1] (Dzz F), then the update, source, receivers,
 // image and state max.  Derivatives of psi_x are taken only within 4
 // columns of a side layer and those of psi_z only within 4 rows of the
@@ -658,7 +734,7 @@ __global__ void __launch_bounds__(kStripBlock) k_fwd_cpml(Batch<float> b, int g,
     if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)s * (b.nt_max + 1) + g + 1]);
 }
 
-// Adjoint, the points k_adj_tma left (after the strip pass and k_adj_tma).
+// Adjoint, the points the layer tiles left (after the strip pass and the layer tiles).
 // One thread per point loops over the active shots of its group in order
 // and adds their imaging to the group's gradient in one read-modify-write.
 //  EXACT: points within 4 of a layer, + Dxx(S ax Zx') - Dx(S ax Yx') (and the
@@ -788,10 +864,10 @@ __global__ void __launch_bounds__(kStripBlock) k_adj_cpml(Batch<float> b, int j,
     }
 }
 
-inline size_t fwd_tma_smem() { return 128 + 2 * sizeof(FwdStage); }
-template <typename S> inline size_t adj_tma_smem()
+inline size_t fwd_tma_smem() { return 128 + kStages * sizeof(FwdStage); }
+inline size_t adj_tma_smem()
 {
-    return 128 + 2 * sizeof(AdjStage<S>) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
+    return 128 + kStages * sizeof(AdjStage) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
 }
 
 }  // namespace fwi
