@@ -198,6 +198,7 @@ def native_arm(args, rank, world, dist):
         J, *_ = ctx.gradient(shots, obs_d, w.mask, out=g_d)
         return J
 
+    ctx.set_tile_timing(True)  # events around the interior tile launches of sampled steps
     for _ in range(args.warmup):
         step()
     clocks = Clocks()
@@ -207,6 +208,7 @@ def native_arm(args, rank, world, dist):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches = 0
     t_fwd = t_adj = t_tot = 0.0
+    tile = np.zeros(4)
     e0.record()
     for _ in range(args.steps):
         J = step()
@@ -214,6 +216,7 @@ def native_arm(args, rank, world, dist):
         t_tot += float(t[0])
         t_fwd += float(t[1])
         t_adj += float(t[2])
+        tile += ctx.last_tile_timing() / args.steps
         launches += ctx.last_launches()
     e1.record()
     torch.cuda.synchronize()
@@ -242,13 +245,18 @@ def native_arm(args, rank, world, dist):
     out = None
     if rank == 0:
         hbm, peak_kind = peaks()
-        # dominant kernel: the adjoint step (strip pass + main pass), timed on its stream
-        pts = sum((s["nxw"] or w.nx) * w.nz * s["nt"] for s in w.w_shots) if hasattr(w, "w_shots") else \
-            sum((s["nxw"] or w.nx) * w.nz * s["nt"] for s in w.shots)
+        # dominant kernel: the adjoint interior tiles (k_adj_tma<.., LAYER=false>), the largest share of
+        # the launch list; per launch: algorithmic bytes (68 B per point update) of the interior points it
+        # updates / its mean duration, from CUDA events on its stream around sampled launches
+        adj_ms, adj_pts = float(tile[2]), float(tile[3])
+        fwd_ms, fwd_pts = float(tile[0]), float(tile[1])
+        kern_gbs = ALG_BYTES_ADJ * adj_pts / (adj_ms / 1e3) / 1e9 if adj_ms > 0 else None
+        fwd_kern_gbs = ALG_BYTES_FWD * fwd_pts / (fwd_ms / 1e3) / 1e9 if fwd_ms > 0 else None
+        # whole phases (all kernels of a step, every point), timed on the context stream
+        pts = sum((s["nxw"] or w.nx) * w.nz * s["nt"] for s in w.shots)
         adj_gbs = ALG_BYTES_ADJ * pts / (t_adj / args.steps / 1e3) / 1e9
         fwd_gbs = ALG_BYTES_FWD * pts / (t_fwd / args.steps / 1e3) / 1e9
-        traffic = traffic_from_profile(f"adjoint_step_{args.workload}_traffic.txt")
-        launches_per_step = 2 * w.nt
+        traffic = traffic_from_profile(f"k_adj_tma_interior_{args.workload}.txt")
         out = {
             "metric": METRIC, "value": round(value, 4), "unit": "shots/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -261,11 +269,18 @@ def native_arm(args, rank, world, dist):
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
                     "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
-            "roofline": {"bound": "hbm", "kernel": "adjoint step (k_adj_strip_exact + k_adj_tma + k_adj_cpml)",
-                         "achieved": round(adj_gbs, 1), "peak": hbm, "unit": "GB/s",
-                         "frac": round(adj_gbs / hbm, 4), "peak_kind": peak_kind,
-                         "traffic": traffic, "forward_step_achieved": round(fwd_gbs, 1),
-                         "forward_frac": round(fwd_gbs / hbm, 4),
+            "roofline": {"bound": "hbm", "kernel": "k_adj_tma interior tiles (adjoint step + imaging)",
+                         "achieved": round(kern_gbs, 1) if kern_gbs else None, "peak": hbm, "unit": "GB/s",
+                         "frac": round(kern_gbs / hbm, 4) if kern_gbs else None, "peak_kind": peak_kind,
+                         "traffic": traffic,
+                         "launch_ms": round(adj_ms, 4), "points_per_launch": int(adj_pts),
+                         "bytes_per_point": ALG_BYTES_ADJ,
+                         "forward_interior": {"achieved": round(fwd_kern_gbs, 1) if fwd_kern_gbs else None,
+                                              "frac": round(fwd_kern_gbs / hbm, 4) if fwd_kern_gbs else None,
+                                              "launch_ms": round(fwd_ms, 4), "points_per_launch": int(fwd_pts),
+                                              "bytes_per_point": ALG_BYTES_FWD},
+                         "adjoint_step_frac": round(adj_gbs / hbm, 4),
+                         "forward_step_frac": round(fwd_gbs / hbm, 4),
                          "gradient_frac": round((ALG_BYTES_FWD + ALG_BYTES_ADJ) * pts / (t_tot / args.steps / 1e3)
                                                 / 1e9 / hbm, 4)},
             "gpu_launches": int(launches),

@@ -178,9 +178,9 @@ __global__ void k_misfit_finish(const double *partial, long n, double *misfit)
     }
 }
 
-// grad[iz][X] += sum over the batch's shot groups of their local gradients
-// (fixed group order); group q holds shots [q sg, (q+1) sg), all with the
-// window of shot q sg.
+// grad[iz][X] += sum over the batch's gradient slots (fixed order); slot q
+// has the window of shot q sg (callers pass sg = 1 when every slot shares
+// one window).
 template <typename T>
 __global__ void k_accumulate_gradient(T *gh, T *gp, T *gn, const T *sh_h, const T *sh_p, const T *sh_n,
                                       const DevShot *shots, int ngroups, int sg, int nx, int nz, int mpitch,
@@ -431,7 +431,36 @@ struct CtxBase {
     int last_cuda = 0;
     float timing[4] = {0, 0, 0, 0};
     long launches = 0;
-    virtual ~CtxBase() {}
+
+    // Interior tile timing (fwi_set_tile_timing): event pairs around the
+    // interior tile launches of up to kTimeSamples sampled steps per phase
+    // (0 forward, 1 adjoint), with the interior points each launch updated.
+    static constexpr int kTimeSamples = 16;
+    bool tile_timing = false;
+    cudaEvent_t tev[2][kTimeSamples][2] = {};
+    double tile_ms[2] = {0, 0}, tile_pts[2] = {0, 0};
+    long tile_n[2] = {0, 0};
+
+    int set_tile_timing(bool on)
+    {
+        if (on && !tev[0][0][0])
+            for (auto &ph : tev)
+                for (auto &pr : ph)
+                    for (auto &e : pr) {
+                        const cudaError_t r = cudaEventCreate(&e);
+                        if (r != cudaSuccess) return fail(r);
+                    }
+        tile_timing = on;
+        return FWI_OK;
+    }
+
+    virtual ~CtxBase()
+    {
+        for (auto &ph : tev)
+            for (auto &pr : ph)
+                for (auto &e : pr)
+                    if (e) cudaEventDestroy(e);
+    }
     virtual int init() = 0;
     virtual int set_model(const void *, const void *, const void *) = 0;
     virtual int set_model_vti(const void *, const void *, const void *) = 0;
@@ -467,7 +496,24 @@ template <typename T> struct Ctx : CtxBase {
     long slot = 0, mslot = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[4] = {};
-    fwi::StepStreams ss{};  // st, plus the side stream of the FP32 strip passes
+    fwi::StepStreams ss{};  // st, plus the side streams of the FP32 step (prop_f32.cu)
+
+
+    // Interior points of the interior tiles of a window nxw wide (tile_role 1 for width aw).
+    long interior_tile_points(int nxw, int aw) const
+    {
+        long n = 0;
+        for (int z0 = 0; z0 < nz; z0 += fwi::kTileEdge)
+            for (int x0 = 0; x0 < nxw; x0 += fwi::kTileEdge)
+                if (fwi::tile_role(x0, z0, nxw, nz, aw) == 1) {
+                    const long w = std::min(x0 + fwi::kTileEdge - 1, nxw - 5) - std::max(x0, 4) + 1;
+                    const long h = std::min(z0 + fwi::kTileEdge - 1, nz - 5) - std::max(z0, 4) + 1;
+                    n += w * h;
+                }
+        return n;
+    }
+
+
     std::vector<void *> allocs;
     // model and setup
     T *vh = nullptr, *vp = nullptr, *vn = nullptr, *mh = nullptr, *mp = nullptr, *mn = nullptr;
@@ -656,6 +702,27 @@ template <typename T> struct Ctx : CtxBase {
         return (int)std::max(1L, std::min(sg, 64L));
     }
 
+    // Shots per group of the layer tiles (with identical windows).  They run
+    // on the side stream beside the interior tiles; the group count gives
+    // about half a wave of adjoint blocks (3 per SM of 152): short enough a
+    // pass, without a block prologue per shot.  Measured on 601 x 301, 32
+    // shots (54 layer tiles): 8 shots per group 60.2 shots/s, 5: 59.1,
+    // 16: 54.9, 2: 56.6, 1: 53.4.
+    int layer_shots_per_group(int nb, int nxm) const
+    {
+        if (const char *e = getenv("FWI_LAYER_SHOTS_PER_GROUP")) {  // tuning override
+            const int v = atoi(e);
+            if (v >= 1) return std::min(v, 64);
+        }
+        long tiles = 0;
+        for (int z0 = 0; z0 < nz; z0 += fwi::kTileEdge)
+            for (int x0 = 0; x0 < nxm; x0 += fwi::kTileEdge)
+                tiles += fwi::tile_role(x0, z0, nxm, nz, cfg.cpml + fwi::kRad) == 2;
+        const long slots = 3L * 152 / 2;
+        const long groups = std::max(1L, std::min((long)nb, (slots + tiles / 2) / std::max(1L, tiles)));
+        return (int)std::max(1L, std::min((nb + groups - 1) / groups, 64L));
+    }
+
     // CPML table by distance (src/main.c:48-51: L = CPML dh, d0 = -3 ln R / (2 L), in T)
     int cpml_table()
     {
@@ -794,6 +861,7 @@ template <typename T> struct Ctx : CtxBase {
         b.img_scale = cfg.mode == FWI_MODE_EXACT ? (T)cfg.dt * (T)cfg.dt : (T)cfg.dt;
         b.status = status;
         b.sg = 1;
+        b.sg_layer = 1;
         b.tma = use_tma ? (const void *)&maps : nullptr;
         return b;
     }
@@ -840,6 +908,7 @@ template <typename T> struct Ctx : CtxBase {
         if (rc) return rc;
         TRY(cudaEventRecord(ev[0], st));
         long launches0 = launches;
+        for (int p = 0; p < 2; p++) { tile_ms[p] = tile_pts[p] = 0; tile_n[p] = 0; }
         const long kps = sizeof(T) == 4 ? 4 : 2;  // kernels per time step (see the file comment)
         if (want_grad)
             for (auto &p : grad) TRY(cudaMemsetAsync(p, 0, mslot * sizeof(T), st));
@@ -870,17 +939,38 @@ template <typename T> struct Ctx : CtxBase {
             TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
             Batch<T> b = batch_view(nb);
             b.sg = shots_per_group(bs, nxm);
+            b.sg_layer = b.sg == 1 ? 1 : layer_shots_per_group(nb, nxm);
             const int ngroups = (nb + b.sg - 1) / b.sg;
+            // gradient slots in use: the interior groups' and the layer tiles' (same window in all)
+            const int nslots = std::max(ngroups, (nb + b.sg_layer - 1) / b.sg_layer);
             cudaEvent_t e0 = ev[1], e1 = ev[2], e2 = ev[3];
             TRY(cudaEventRecord(e0, st));
             const bool ckpt = want_grad && cfg.store == FWI_STORE_CHECKPOINT;
+            // sampled steps of the interior tile timing: events and interior points updated
+            const bool timed = tile_timing && sizeof(T) == 4;
+            const int tstride = std::max(1, ntb / kTimeSamples);
+            int nsamp[2] = {0, 0};
+            double spts[2][kTimeSamples];
+            auto sample = [&](int phase, int step, fwi::StepStreams &sst) {
+                if (!timed || step % tstride != tstride / 2 || nsamp[phase] >= kTimeSamples) return;
+                const int aw = phase == 0 || !exact ? cfg.cpml : cfg.cpml + fwi::kRad;
+                double pts = 0;
+                for (const DevShot &d : bs)
+                    if (phase == 0 ? step - (ntb - d.nt) >= 0 : step < d.nt) pts += (double)interior_tile_points(d.nx, aw);
+                const int k = nsamp[phase]++;
+                spts[phase][k] = pts;
+                sst.t0 = tev[phase][k][0];
+                sst.t1 = tev[phase][k][1];
+            };
             int cur = 0;
             for (int g = 0; g < ntb; g++) {
                 if (ckpt && g % ck_every == 0) {
                     int rc2 = save_checkpoint(g / ck_every, nb, cur);
                     if (rc2) return rc2;
                 }
-                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt) ? g : -1, exact, ss);
+                fwi::StepStreams sst = ss;
+                sample(0, g, sst);
+                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt) ? g : -1, exact, sst);
                 cur ^= 1;
             }
             TRY_LAUNCH();
@@ -903,7 +993,9 @@ template <typename T> struct Ctx : CtxBase {
                 int zsel = 0;
                 if (!ckpt) {
                     for (int j = 0; j < ntb; j++) {
-                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, ss);
+                        fwi::StepStreams sst = ss;
+                        sample(1, j, sst);
+                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, sst);
                         cur ^= 1;
                         zsel ^= 1;
                     }
@@ -933,7 +1025,9 @@ template <typename T> struct Ctx : CtxBase {
                         }
                         launches += kps * (e - a);
                         for (; j < ntb && ntb - 1 - lag - j >= a; j++) {
-                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a, ss);
+                            fwi::StepStreams sst = ss;
+                            sample(1, j, sst);
+                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a, sst);
                             cur ^= 1;
                             zsel ^= 1;
                             launches += kps;
@@ -948,8 +1042,7 @@ template <typename T> struct Ctx : CtxBase {
                     TRY_LAUNCH();
                 }
                 k_accumulate_gradient<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(
-                    grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, ngroups, b.sg, nx, nz, mpitch, pitch,
-                    slot);
+                    grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, nslots, 1, nx, nz, mpitch, pitch, slot);
                 TRY_LAUNCH();
                 launches++;
             }
@@ -960,6 +1053,14 @@ template <typename T> struct Ctx : CtxBase {
             cudaEventElapsedTime(&c, e1, e2);
             t_fwd += a;
             t_adj += c;
+            for (int p = 0; p < 2; p++)
+                for (int k = 0; k < nsamp[p]; k++) {
+                    float ms = 0;
+                    TRY(cudaEventElapsedTime(&ms, tev[p][k][0], tev[p][k][1]));
+                    tile_ms[p] += ms;
+                    tile_pts[p] += spts[p][k];
+                    tile_n[p]++;
+                }
         }
         unsigned stat = 0;
         TRY(cudaMemcpyAsync(&stat, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -1302,6 +1403,24 @@ int fwi_lbfgs_update(void *ctx, float av, float ad, float ae, int fmin, int fmax
 }
 int fwi_restore_model(void *ctx) { return ctx ? as_ctx(ctx)->restore_model() : FWI_ERR_ARG; }
 int fwi_gradient_vti(void *ctx, void *a, void *b, void *c) { return ctx ? as_ctx(ctx)->gradient_vti(a, b, c) : FWI_ERR_ARG; }
+
+int fwi_set_tile_timing(void *ctx, int on)
+{
+    if (!ctx) return FWI_ERR_ARG;
+    return as_ctx(ctx)->set_tile_timing(on != 0);
+}
+
+int fwi_last_tile_timing(void *ctx, double *out4)
+{
+    if (!ctx || !out4) return FWI_ERR_ARG;
+    CtxBase *c = as_ctx(ctx);
+    for (int p = 0; p < 2; p++) {
+        const long n = c->tile_n[p];
+        out4[2 * p] = n ? c->tile_ms[p] / n : 0.0;
+        out4[2 * p + 1] = n ? c->tile_pts[p] / n : 0.0;
+    }
+    return FWI_OK;
+}
 
 int fwi_last_timing(void *ctx, float *out4)
 {

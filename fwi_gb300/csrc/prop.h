@@ -42,6 +42,8 @@ template <typename T> struct Batch {
     unsigned *status;       // bit 0: stored image saturated, bit 1: a pipeline wait gave up
     int sg;                 // shots per group: shots [q sg, (q+1) sg) share a window, and
                             // g[k] + q * slot accumulates the imaging of group q
+    int sg_layer;           // the same for the FP32 layer tiles (their points are disjoint
+                            // from the other passes', so the slots do not collide)
     const void *tma;        // host copy of the batch's TMA tensor maps (FP32 path), or null
 };
 
@@ -56,6 +58,29 @@ template <typename T> struct Batch {
 // reference's leapfrog; in FP32 it keeps the low bits of each small update
 // that 2 u^n - u^{n-1} + dt^2 (...) rounds away.
 
+// Tiles of the FP32 tile passes: kTileEdge x kTileEdge points.
+constexpr int kTileEdge = 32;
+
+// Points the CPML layers touch.  `aw` is the CPML width (forward, reference
+// adjoint) or CPML width + 4 (exact adjoint, whose transpose terms reach 4
+// points further).  Same shape as the reference's strip predicate
+// (src/parallelcalls.cu:55).
+__host__ __device__ inline bool layer_point(int ix, int iz, int nx, int nz, int aw)
+{
+    return ix < aw || ix > nx - aw - 1 || iz > nz - aw - 1;
+}
+
+// Role of the tile at (x0, z0) of an nx x nz window: 0 no interior point,
+// 1 interior tile (no layer point), 2 layer tile.
+__host__ __device__ inline int tile_role(int x0, int z0, int nx, int nz, int aw)
+{
+    if (x0 > nx - 5 || z0 > nz - 5) return 0;
+    const int xa = x0 > 4 ? x0 : 4;
+    const int xb = x0 + kTileEdge - 1 < nx - 5 ? x0 + kTileEdge - 1 : nx - 5;
+    const int zb = z0 + kTileEdge - 1 < nz - 5 ? z0 + kTileEdge - 1 : nz - 5;
+    return (xa < aw || xb > nx - aw - 1 || zb > nz - aw - 1) ? 2 : 1;
+}
+
 // Streams of a step.  The FP32 path runs the interior tiles on `main`, the
 // layer tiles on `side` and the strip pass (CPML memory variables) on
 // `strip`, all three from the current time level; the layer points follow on
@@ -64,6 +89,7 @@ template <typename T> struct Batch {
 struct StepStreams {
     cudaStream_t main = nullptr, side = nullptr, strip = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, strip_done = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;  // if set: recorded on `main` around the interior tiles
 };
 
 // Forward global step g.  `cur` is the level holding each shot's current

@@ -18,9 +18,9 @@ template <typename K> void allow_smem(K kernel, size_t bytes)
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-inline dim3 tma_grid(const Batch<float> &b, int nx_max)
+inline dim3 tma_grid(const Batch<float> &b, int nx_max, int sg)
 {
-    return dim3((nx_max + TT - 1) / TT, (b.nz + TT - 1) / TT, (b.B + b.sg - 1) / b.sg);
+    return dim3((nx_max + TT - 1) / TT, (b.nz + TT - 1) / TT, (b.B + sg - 1) / sg);
 }
 
 // Layer-point kernels: enough blocks for every point of the widest window, `ny` in y.
@@ -38,8 +38,9 @@ void fwd_tiles(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int s
     static bool set = false;
     const size_t sm = fwd_tma_smem();
     if (!set) { allow_smem(k_fwd_tma<ST, EXACT, LAYER>, sm); set = true; }
-    k_fwd_tma<ST, EXACT, LAYER><<<tma_grid(b, nx_max), kTmaThreads, sm, st>>>(
-        b, *static_cast<const TmaMaps *>(b.tma), g, ntb, cur, slot, b.sg);
+    const int sg = LAYER ? b.sg_layer : b.sg;
+    k_fwd_tma<ST, EXACT, LAYER><<<tma_grid(b, nx_max, sg), kTmaThreads, sm, st>>>(
+        b, *static_cast<const TmaMaps *>(b.tma), g, ntb, cur, slot, sg);
 }
 
 template <int ST, bool EXACT, bool LAYER>
@@ -48,8 +49,9 @@ void adj_tiles(const Batch<float> &b, int nx_max, int j, int ntb, int cur, int z
     static bool set = false;
     const size_t sm = adj_tma_smem();
     if (!set) { allow_smem(k_adj_tma<ST, EXACT, LAYER>, sm); set = true; }
-    k_adj_tma<ST, EXACT, LAYER><<<tma_grid(b, nx_max), kTmaThreads, sm, st>>>(
-        b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, img_base, b.sg);
+    const int sg = LAYER ? b.sg_layer : b.sg;
+    k_adj_tma<ST, EXACT, LAYER><<<tma_grid(b, nx_max, sg), kTmaThreads, sm, st>>>(
+        b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, img_base, sg);
 }
 
 // The forward tiles compute the same thing in both modes (the points they
@@ -121,7 +123,9 @@ void fork_join(const StepStreams &ss, Strip strip_work, Layer layer_work, Points
     cudaStreamWaitEvent(ss.side, ss.strip_done, 0);
     point_work(ss.side);
     cudaEventRecord(ss.join, ss.side);
+    if (ss.t0) cudaEventRecord(ss.t0, ss.main);
     interior_work(ss.main);
+    if (ss.t1) cudaEventRecord(ss.t1, ss.main);
     cudaStreamWaitEvent(ss.main, ss.join, 0);
 }
 

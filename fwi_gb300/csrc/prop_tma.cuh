@@ -24,7 +24,7 @@
 
 namespace fwi {
 
-constexpr int TT = 32;             // tile edge
+constexpr int TT = kTileEdge;      // tile edge
 constexpr int TH = TT + 2 * kRad;  // tile with a 4-point halo on every side (40)
 constexpr int kTmaThreads = 256;   // 8 threads x 4 points per row, 32 rows
 constexpr int kMaxGroup = 64;
@@ -51,23 +51,6 @@ struct AdjStage {
 };
 
 constexpr int kStages = 3;  // TMA pipeline depth over a group's shots
-
-// Points the layers touch.  `aw` is the CPML width (forward, reference
-// adjoint) or CPML width + 4 (exact adjoint, whose transpose terms reach 4
-// points further).  Same shape as the reference's strip predicate.
-__device__ __forceinline__ bool layer_point(int ix, int iz, int nx, int nz, int aw)
-{
-    return ix < aw || ix > nx - aw - 1 || iz > nz - aw - 1;
-}
-
-// Role of the tile at (x0, z0): 0 no interior point, 1 interior tile (no
-// layer point), 2 layer tile.
-__device__ __forceinline__ int tile_role(int x0, int z0, int nx, int nz, int aw)
-{
-    if (x0 > nx - 5 || z0 > nz - 5) return 0;
-    const int xa = max(x0, 4), xb = min(x0 + TT - 1, nx - 5), zb = min(z0 + TT - 1, nz - 5);
-    return (xa < aw || xb > nx - aw - 1 || zb > nz - aw - 1) ? 2 : 1;
-}
 
 __device__ __forceinline__ unsigned char *aligned_dsm(unsigned char *p)
 {

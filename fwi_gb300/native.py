@@ -107,6 +107,8 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_restore_model", [_p])
         _sig(L, "fwi_gradient_vti", [_p, _p, _p, _p])
         _sig(L, "fwi_last_timing", [_p, _p])
+        _sig(L, "fwi_set_tile_timing", [_p, _i])
+        _sig(L, "fwi_last_tile_timing", [_p, _p])
         _sig(L, "fwi_last_launches", [_p], _l)
         _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
         _sig(L, "fwi_residual_misfit_noalloc", [_p, _p, _p, _p, _l, _i, _p, _p])
@@ -342,3 +344,12 @@ class Context:
 
     def last_launches(self):
         return int(lib().fwi_last_launches(self._h))
+
+    def set_tile_timing(self, on=True):
+        _check(lib().fwi_set_tile_timing(self._h, 1 if on else 0), "fwi_set_tile_timing")
+
+    def last_tile_timing(self):
+        """(forward ms, forward points, adjoint ms, adjoint points) per interior tile launch."""
+        t = np.zeros(4, np.float64)
+        _check(lib().fwi_last_tile_timing(self._h, t.ctypes.data), "fwi_last_tile_timing")
+        return t

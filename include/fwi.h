@@ -190,6 +190,16 @@ int fwi_gradient_vti(void *ctx, void *g_vp, void *g_eps, void *g_delta);
  * out[0] total, out[1] forward, out[2] adjoint, out[3] other. */
 int fwi_last_timing(void *ctx, float *out4);
 
+/* Per-launch timing of the interior tile kernels (no counterpart in the
+ * reference).  With on != 0, later fwi_gradient / fwi_misfit / fwi_forward
+ * calls record CUDA events on the launching stream around the interior tile
+ * launch of up to 16 sampled time steps per phase (FP32 contexts only).
+ * fwi_last_tile_timing: out[0] mean forward launch duration (ms), out[1]
+ * interior points it updated (summed over the batch's shots), out[2], out[3]
+ * the same for the adjoint; zeros when nothing was sampled. */
+int fwi_set_tile_timing(void *ctx, int on);
+int fwi_last_tile_timing(void *ctx, double *out4);
+
 /* How many of this library's kernels the last call launched. */
 long fwi_last_launches(void *ctx);
 
