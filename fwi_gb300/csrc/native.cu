@@ -2,11 +2,11 @@
 //
 // One context = one device, one stream, one arena of device memory.  A
 // gradient call runs the shots in batches of up to max_shots:
-//   forward (FP32: strip pass, layer tiles and layer points on a side stream
-//   beside the interior tiles, 4 launches / step; FP64: 2), images kept per
-//   the storage mode
+//   forward (FP32: strip pass and layer tiles on a side stream beside the
+//   interior tiles, 3 launches / step; FP64: 2), images kept per the
+//   storage mode
 //   -> residual + FP64 misfit partials
-//   -> adjoint + imaging (4 launches / step in FP32, 2 in FP64)
+//   -> adjoint + imaging (3 launches / step in FP32, 2 in FP64)
 //   -> deterministic reduction of the per-shot gradients into the model grid.
 // The L-BFGS update of src/main.c:539-800 runs on the device with FP64 dot
 // products reduced by the last block to finish (no host round trip).
@@ -65,6 +65,8 @@ struct HostTmaMaps {
     CUtensorMap lvl[4];
     CUtensorMap px[2];
     CUtensorMap fz[2];
+    CUtensorMap mx[8];
+    CUtensorMap mz[8];
 };
 
 }  // namespace fwi
@@ -521,7 +523,7 @@ template <typename T> struct Ctx : CtxBase {
     bool have_model = false, have_wavelet = false, models_dirty = true;
     int wavelet_nt = 0;
     // batch
-    T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {}, *scr[4] = {};
+    T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {};
     void *store = nullptr;
     // checkpointing: full states every ck_every steps, segment recompute buffers
     int ck_every = 0, n_ck = 0;
@@ -553,13 +555,11 @@ template <typename T> struct Ctx : CtxBase {
         if (st) cudaStreamSynchronize(st);
         for (void *p : allocs) cudaFree(p);
         if (ss.side) cudaStreamSynchronize(ss.side);
-        if (ss.strip) cudaStreamSynchronize(ss.strip);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
-        for (cudaEvent_t e : {ss.fork, ss.join, ss.strip_done})
+        for (cudaEvent_t e : {ss.fork, ss.join})
             if (e) cudaEventDestroy(e);
         if (ss.side) cudaStreamDestroy(ss.side);
-        if (ss.strip) cudaStreamDestroy(ss.strip);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -599,23 +599,19 @@ template <typename T> struct Ctx : CtxBase {
         ss.main = st;
         if (sizeof(T) == 4) {
             // the side stream carries the step's critical path (strip pass -> layer
-            // tiles -> layer points): the highest priority, so that its blocks take
-            // SM slots ahead of the interior tiles' as those free up
+            // tiles): the highest priority, so that its blocks take SM slots ahead
+            // of the interior tiles' as those free up
             int lo = 0, hi = 0;
             TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
             TRY(cudaStreamCreateWithPriority(&ss.side, cudaStreamNonBlocking, hi));
-            TRY(cudaStreamCreateWithPriority(&ss.strip, cudaStreamNonBlocking, hi));
             TRY(cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming));
             TRY(cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming));
-            TRY(cudaEventCreateWithFlags(&ss.strip_done, cudaEventDisableTiming));
         }
         for (T **p : {&vh, &vp, &vn, &mh, &mp, &mn}) TRY(alloc(p, mslot));
         TRY(alloc(&cpa, cfg.cpml + 1));
         TRY(alloc(&cpb, cfg.cpml + 1));
         TRY(alloc(&wavelet, nt_max));
         for (auto &p : lvl) TRY(alloc(&p, (size_t)B * slot));
-        if (sizeof(T) == 4)
-            for (auto &p : scr) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : cp) TRY(alloc(&p, (size_t)B * slot));
         for (auto &p : gs) TRY(alloc(&p, (size_t)B * slot));
         if (cfg.store == FWI_STORE_CHECKPOINT) {
@@ -633,8 +629,12 @@ template <typename T> struct Ctx : CtxBase {
             store = q0;
         }
         if (sizeof(T) == sizeof(float)) {
-            int rc = build_maps(maps, lvl) ;
-            if (rc == FWI_OK && cfg.store == FWI_STORE_CHECKPOINT) rc = build_maps(rmaps, rlvl);
+            int rc = build_maps(maps, lvl, cp);
+            if (rc == FWI_OK && cfg.store == FWI_STORE_CHECKPOINT) {
+                // the recompute's forward steps use its own first 4 CPML arrays
+                T *const rcpv[8] = {rcp[0], rcp[1], rcp[2], rcp[3], cp[4], cp[5], cp[6], cp[7]};
+                rc = build_maps(rmaps, rlvl, rcpv);
+            }
             if (rc != FWI_OK) return rc;
             use_tma = true;
         }
@@ -664,7 +664,7 @@ template <typename T> struct Ctx : CtxBase {
         return FWI_OK;
     }
 
-    int build_maps(fwi::HostTmaMaps &m, T *const (&lv)[6])
+    int build_maps(fwi::HostTmaMaps &m, T *const (&lv)[6], T *const (&cpv)[8])
     {
         using namespace fwi;
         for (int k = 0; k < 4; k++) {
@@ -675,6 +675,12 @@ template <typename T> struct Ctx : CtxBase {
             int rc = make_tensor_map_3d(&m.px[k], lv[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 40, 32, 1);
             if (rc) return rc;
             rc = make_tensor_map_3d(&m.fz[k], lv[2 + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 32, 40, 1);
+            if (rc) return rc;
+        }
+        for (int k = 0; k < 8; k++) {  // CPML memory variables, both halo shapes (layer tiles)
+            int rc = make_tensor_map_3d(&m.mx[k], cpv[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 40, 32, 1);
+            if (rc) return rc;
+            rc = make_tensor_map_3d(&m.mz[k], cpv[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 32, 40, 1);
             if (rc) return rc;
         }
         return FWI_OK;
@@ -850,7 +856,6 @@ template <typename T> struct Ctx : CtxBase {
         b.B = nb; b.nz = nz; b.pitch = pitch; b.mpitch = mpitch; b.cpml = cfg.cpml; b.nt_max = nt_max;
         b.slot = slot;
         for (int k = 0; k < 6; k++) b.lvl[k] = lvl[k];
-        for (int k = 0; k < 4; k++) b.scr[k] = scr[k];
         for (int k = 0; k < 8; k++) b.cp[k] = cp[k];
         for (int k = 0; k < 3; k++) b.g[k] = gs[k];
         b.store = store; b.store_type = store_type(); b.n_img = n_img;
@@ -909,7 +914,7 @@ template <typename T> struct Ctx : CtxBase {
         TRY(cudaEventRecord(ev[0], st));
         long launches0 = launches;
         for (int p = 0; p < 2; p++) { tile_ms[p] = tile_pts[p] = 0; tile_n[p] = 0; }
-        const long kps = sizeof(T) == 4 ? 4 : 2;  // kernels per time step (see the file comment)
+        const long kps = sizeof(T) == 4 ? 3 : 2;  // kernels per time step (see the file comment)
         if (want_grad)
             for (auto &p : grad) TRY(cudaMemsetAsync(p, 0, mslot * sizeof(T), st));
         TRY(cudaMemsetAsync(misfit, 0, sizeof(double), st));
@@ -1295,7 +1300,7 @@ size_t fwi_config_bytes(const fwi_config *c)
     const long nrec = c->max_receivers > 0 ? c->max_receivers : win;
     size_t b = 0;
     b += (size_t)(6 + 3 + 12) * mslot * e;                 // models, gradient, L-BFGS work arrays
-    b += (size_t)c->max_shots * slot * e * (6 + 8 + 3 + (e == 4 ? 4 : 0));  // levels, CPML state, gradients, FP32 scratch
+    b += (size_t)c->max_shots * slot * e * (6 + 8 + 3);  // levels, CPML state, gradients
     if (c->store == FWI_STORE_CHECKPOINT) {
         const long k = checkpoint_interval(*c), n = (c->nt_max + k - 1) / k;
         b += (size_t)c->max_shots * slot * e * (8 * n + 10); // checkpoints, recompute state

@@ -24,7 +24,6 @@ template <typename T> struct Batch {
     int B, nz, pitch, mpitch, cpml, nt_max;
     long slot;
     T *lvl[6];      // P level 0, P level 1, F level 0, F level 1, P increment, F increment
-    T *scr[4];      // per-shot scratch: stencil values of layer points, layer tiles -> layer kernels
     T *cp[8];       // CPML memory variables (forward uses 0..3)
     T *g[3];        // per-shot gradient accumulators: v_hor, v_po, v_nmo
     void *store;    // images: [B][n_img][2][slot] of the store type
@@ -81,14 +80,14 @@ __host__ __device__ inline int tile_role(int x0, int z0, int nx, int nz, int aw)
     return (xa < aw || xb > nx - aw - 1 || zb > nz - aw - 1) ? 2 : 1;
 }
 
-// Streams of a step.  The FP32 path runs the interior tiles on `main`, the
-// layer tiles on `side` and the strip pass (CPML memory variables) on
-// `strip`, all three from the current time level; the layer points follow on
-// `side` once the strip pass is done, and `main` joins `side` before the next
-// step.  side == nullptr: everything on `main` (as the FP64 path does).
+// Streams of a step.  The FP32 path runs the interior tiles on `main` and
+// the strip pass (CPML memory variables) followed by the layer tiles on
+// `side`, both from the current time level, and `main` joins `side` before
+// the next step.  side == nullptr: everything on `main` (as the FP64 path
+// does).
 struct StepStreams {
-    cudaStream_t main = nullptr, side = nullptr, strip = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, strip_done = nullptr;
+    cudaStream_t main = nullptr, side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr;  // if set: recorded on `main` around the interior tiles
 };
 

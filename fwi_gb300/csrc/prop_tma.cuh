@@ -10,13 +10,8 @@
 // sums the imaging of its group in registers (one gradient read-modify-write
 // per group and step).
 //
-// The tiles split in two launches of the same kernel template:
-//  * interior tiles (LAYER = false): no point the CPML layers touch;
-//  * layer tiles (LAYER = true): the CPML terms of their layer points too,
-//    from the memory variables the strip pass of the step has advanced.
-// Both read only the current time level and write disjoint points, so the
-// host runs [strip pass -> layer tiles] on a side stream concurrently with
-// the interior tiles.
+// These kernels take the interior tiles (tile_role 1: no point the CPML
+// layers touch); prop_layer.cuh takes the layer tiles.
 #pragma once
 
 #include "prop.cuh"
@@ -29,17 +24,19 @@ constexpr int TH = TT + 2 * kRad;  // tile with a 4-point halo on every side (40
 constexpr int kTmaThreads = 256;   // 8 threads x 4 points per row, 32 rows
 constexpr int kMaxGroup = 64;
 
-// Tensor maps over one batch's per-shot arrays ([B][nz][pitch]) and images.
+// Tensor maps over one batch's per-shot arrays ([B][nz][pitch]).
 struct TmaMaps {
     CUtensorMap lvl[4];  // P level 0/1, F level 0/1: 40 x 40 boxes
     CUtensorMap px[2];   // P level 0/1: 40 x 32 boxes (x-halo)
     CUtensorMap fz[2];   // F level 0/1: 32 x 40 boxes (z-halo)
+    CUtensorMap mx[8];   // CPML memory variables cp[k]: 40 x 32 boxes (x-halo)
+    CUtensorMap mz[8];   // the same, 32 x 40 boxes (z-halo)
 };
 
-// The forward operator takes Dxx of P and Dzz of F only: each is staged
-// with the halo along its own axis.
 // Only the fields read with a halo are staged; the increments and images,
 // read at each thread's own 4 points, are loaded straight into registers.
+// The forward operator takes Dxx of P and Dzz of F only: each is staged with
+// the halo along its own axis.
 struct FwdStage {
     float P[TT][TH];
     float F[TH][TT];
@@ -79,14 +76,15 @@ __device__ __forceinline__ bool stage_ready(uint64_t *bar, unsigned parity, unsi
 }
 
 // After a failed wait at shot a: give the loads still in flight (shots a + 1
-// .. a + kStages - 1) a bounded time to land before the block's shared memory
-// is released.
-__device__ __forceinline__ void drain_stages(uint64_t *bar, int a, int na)
+// .. a + nst - 1 of an nst-stage pipeline) a bounded time to land before the
+// block's shared memory is released.
+__device__ __forceinline__ void drain_stages_n(uint64_t *bar, int a, int na, int nst)
 {
     if (threadIdx.x == 0)
-        for (int k = a + 1; k < min(a + kStages, na); k++) (void)mbar_wait(&bar[k % kStages], (k / kStages) & 1);
+        for (int k = a + 1; k < min(a + nst, na); k++) (void)mbar_wait(&bar[k % nst], (k / nst) & 1);
     __syncthreads();
 }
+__device__ __forceinline__ void drain_stages(uint64_t *bar, int a, int na) { drain_stages_n(bar, a, na, kStages); }
 
 __device__ __forceinline__ int active_shots(const Batch<float> &b, int sg, int *act, bool adjoint, int step, int ntb)
 {
@@ -176,7 +174,8 @@ struct FwdShot {
     float w, sc;    // wavelet sample, image scale
 };
 
-template <int ST, bool EXACT, bool LAYER>  // EXACT: unused (see the launcher)
+// Interior tiles: no CPML term, so the images are the plain stencils in both modes.
+template <int ST>
 __global__ void __launch_bounds__(kTmaThreads, 4)
 k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, int cur, int img_slot, int sg)
 {
@@ -190,7 +189,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
     const DevShot gsh = b.shots[blockIdx.z * sg];  // every shot of the group has this window
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
-    if (tile_role(x0, z0, nx, nz, cpml) != (LAYER ? 2 : 1)) return;
+    if (tile_role(x0, z0, nx, nz, cpml) != 1) return;
     const int na = active_shots(b, sg, act, false, g, ntb);
     if (na == 0) return;
     if (tid == 0) {
@@ -227,18 +226,15 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
         for (int k = 0; k < min(kStages, na); k++) issue(k);
     const int c4 = 4 * (tid & 7), r = tid >> 3;
     const int ix0 = x0 + c4, iz = z0 + r;
-    bool m[4], L[4];  // points finished here, layer points (layer tiles: stencils to scratch)
-    bool any = false, all = true, anyL = false;
+    bool m[4];  // interior points
+    bool any = false, all = true;
     float mh[4], mp[4], mn[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int ix = ix0 + q;
-        const bool in = ix < nx && iz < nz && interior(ix, iz, nx, nz);
-        L[q] = LAYER && in && layer_point(ix, iz, nx, nz, cpml);
-        m[q] = in && !L[q];
+        m[q] = ix < nx && iz < nz && interior(ix, iz, nx, nz);
         any |= m[q];
         all &= m[q];
-        anyL |= L[q];
         const long mi = (long)iz * b.mpitch + gsh.x0 + ix;
         mh[q] = m[q] ? b.mh[mi] : 0.f;
         mp[q] = m[q] ? b.mp[mi] : 0.f;
@@ -261,7 +257,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
         }
         const FwdStage &S = stage[a % kStages];
         float lmax = 0.f;
-        if (any || anyL) {
+        if (any) {
             float pv[12];
             {
                 const float *row = &S.P[r][c4];
@@ -280,14 +276,6 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
             for (int q = 0; q < 4; q++) {
                 gG[q] = d2_row(pv, q) * b.inv_dh2;
                 gH[q] = d2_col(fz, q) * b.inv_dh2;
-            }
-            if (LAYER && anyL) {  // Dxx P, Dzz F of the layer points, for k_fwd_cpml
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (L[q]) {
-                        b.scr[0][so + ipt + q] = gG[q];
-                        b.scr[1][so + ipt + q] = gH[q];
-                    }
             }
             float nP[4], nF[4], iP[4], iF[4];
 #pragma unroll
@@ -360,36 +348,6 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
 
 // ------------------------------------------------------------------ adjoint tiles
 
-// Reference adjoint, layer point: the four second derivatives of the
-// model-weighted fields (src/parallelcalls.cu:200-214), kept apart because
-// the zeta recursion needs them, from the tile's staged fields and model
-// tiles to scratch (k_adj_cpml reads them).  (c, r): column and row in the tile.
-struct Scr4 {
-    float *p[4];
-    float inv_dh2;
-};
-
-__device__ __noinline__ void ref_layer_stencils(const Scr4 &o, long i, int c, int r, const float (*MH)[TH],
-                                                const float (*MN)[TH], const float (*MP)[TT], const float (*P)[TH],
-                                                const float (*F)[TH])
-{
-    using C = Coef<float>;
-    const float c2[5] = {C::d2_0, C::d2_1, -C::d2_2, C::d2_3, -C::d2_4};
-    float p2cx = 0.f, r2dx = 0.f, p2cz = 0.f, r2cz = 0.f;
-#pragma unroll
-    for (int k = -4; k <= 4; k++) {
-        const float w2 = c2[k < 0 ? -k : k];
-        p2cx += w2 * (MH[r][c + kRad + k] * P[r + kRad][c + kRad + k]);
-        r2dx += w2 * (MN[r][c + kRad + k] * F[r + kRad][c + kRad + k]);
-        p2cz += w2 * (MP[r + kRad + k][c] * P[r + kRad + k][c + kRad]);
-        r2cz += w2 * (MP[r + kRad + k][c] * F[r + kRad + k][c + kRad]);
-    }
-    o.p[0][i] = p2cx * o.inv_dh2;
-    o.p[1][i] = r2dx * o.inv_dh2;
-    o.p[2][i] = p2cz * o.inv_dh2;
-    o.p[3][i] = r2cz * o.inv_dh2;
-}
-
 // Per-shot scalars of an adjoint step, gathered once per block.
 struct AdjShot {
     long so;        // shot offset in the per-shot arrays
@@ -399,7 +357,7 @@ struct AdjShot {
     float inv_sc;   // inverse image scale
 };
 
-template <int ST, bool EXACT, bool LAYER>
+template <int ST, bool EXACT>
 __global__ void __launch_bounds__(kTmaThreads, 3)
 k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int zsel, int img_base,
           int sg)
@@ -424,7 +382,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     const DevShot gsh = b.shots[grp * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
     const int aw = EXACT ? cpml + kRad : cpml;
-    if (tile_role(x0, z0, nx, nz, aw) != (LAYER ? 2 : 1)) return;
+    if (tile_role(x0, z0, nx, nz, aw) != 1) return;
     const int na = active_shots(b, sg, act, true, j, ntb);
     if (na == 0) return;
     const int lag = EXACT ? 0 : 1;
@@ -474,17 +432,14 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     }
     const int c4 = 4 * (tid & 7), r = tid >> 3;
     const int ix0 = x0 + c4, iz = z0 + r;
-    bool m[4], L[4];  // points finished here, points the layers touch (layer tiles: stencils to scratch)
-    bool any = false, all = true, anyL = false;
+    bool m[4];  // interior points
+    bool any = false, all = true;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int ix = ix0 + q;
-        const bool in = ix < nx && iz < nz && interior(ix, iz, nx, nz);
-        L[q] = LAYER && in && layer_point(ix, iz, nx, nz, aw);
-        m[q] = in && !L[q];
+        m[q] = ix < nx && iz < nz && interior(ix, iz, nx, nz);
         any |= m[q];
         all &= m[q];
-        anyL |= L[q];
     }
     const long ipt = (long)iz * pitch + ix0;
     float *const lPn0 = b.lvl[1 - cur], *const lFn0 = b.lvl[3 - cur];
@@ -526,32 +481,6 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
         __syncthreads();
         const AdjShot &sh = ps[a];
         const long so = sh.so;
-        if (LAYER && anyL) {
-            // stencil values of the layer points, for k_adj_cpml
-            if (EXACT) {
-                float uv[12];
-                const float4 a0 = ld4(&U[r][c4]), a1 = ld4(&U[r][c4 + 4]), a2 = ld4(&U[r][c4 + 8]);
-                uv[0] = a0.x; uv[1] = a0.y; uv[2] = a0.z; uv[3] = a0.w;
-                uv[4] = a1.x; uv[5] = a1.y; uv[6] = a1.z; uv[7] = a1.w;
-                uv[8] = a2.x; uv[9] = a2.y; uv[10] = a2.z; uv[11] = a2.w;
-                float4 vz[9];
-#pragma unroll
-                for (int k = 0; k < 9; k++) vz[k] = ld4(&V[r + k][c4]);
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (L[q]) {
-                        b.scr[0][so + ipt + q] = d2_row(uv, q) * b.inv_dh2;
-                        b.scr[1][so + ipt + q] = d2_col(vz, q) * b.inv_dh2;
-                    }
-            } else {
-                Scr4 o;
-                for (int k = 0; k < 4; k++) o.p[k] = b.scr[k];
-                o.inv_dh2 = b.inv_dh2;
-#pragma unroll 1
-                for (int q = 0; q < 4; q++)
-                    if (L[q]) ref_layer_stencils(o, so + ipt + q, c4 + q, r, MH, MN, MP, S.P, S.F);
-            }
-        }
         if (any) {
             float uv[12];
             {
@@ -638,212 +567,6 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                 g1[q] += ap[q];
                 g2[q] += an[q];
             }
-    }
-}
-
-// ------------------------------------------------------------------ layer points
-
-// Forward, points inside the layers (after the strip pass and the layer
-// tiles): the zeta recursion and the memory-variable derivatives of
-// src/parallelcalls.cu:55-84 on the stencil values the layer tiles left in
-// scr[0] (Dxx P) and scr[1] (Dzz F), then the update, source, receivers,
-// image and state max.  Derivatives of psi_x are taken only within 4
-// columns of a side layer and those of psi_z only within 4 rows of the
-// bottom one: elsewhere every term is exactly zero.
-template <int ST, bool EXACT>
-__global__ void __launch_bounds__(kStripBlock) k_fwd_cpml(Batch<float> b, int g, int ntb, int cur, int img_slot)
-{
-    using Cd = Codec<float, ST>;
-    const int s = blockIdx.y;
-    const DevShot sh = b.shots[s];
-    const int it = g - (ntb - sh.nt);
-    if (it < 0) return;
-    const int nx = sh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
-    const StripMap smap = StripMap::make(nx, nz, cpml);
-    const long so = (long)s * b.slot;
-    const float *P = b.lvl[cur] + so, *F = b.lvl[2 + cur] + so;
-    float *Pn = b.lvl[1 - cur] + so, *Fn = b.lvl[3 - cur] + so;
-    float *Pv = b.lvl[4] + so, *Fv = b.lvl[5] + so;
-    const float *psx = b.cp[0] + so, *psz = b.cp[1] + so;
-    float *zx = b.cp[2] + so, *zz = b.cp[3] + so;
-    const float *p2s = b.scr[0] + so, *r2s = b.scr[1] + so;
-    float sc = 1.f;
-    typename Cd::S *img = nullptr;
-    if (img_slot >= 0) {
-        img = (typename Cd::S *)b.store + ((long)s * b.n_img + img_slot) * 2 * b.slot;
-        if (Cd::scaled) sc = image_scale(b.amax[(long)s * (b.nt_max + 1) + g], (float)b.inv_dh2);
-    }
-    const float w = b.wavelet[it];
-    const int nrec = sh.rx1 - sh.rx0;
-    float lmax = 0.f;
-    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < smap.count();
-         k += (long)gridDim.x * blockDim.x) {
-        int ix, iz;
-        smap.point(k, ix, iz);
-        const long i = (long)iz * pitch + ix;
-        const float p2 = p2s[i], r2 = r2s[i];
-        float G = p2, H = r2;
-        {
-            const bool xl = ix < cpml || ix > nx - cpml - 1;
-            const float tx = (ix < cpml + kRad || ix > nx - cpml - 1 - kRad) ? d1_strided(psx, i, 1) * b.inv_dh : 0.f;
-            const float zxn = xl ? coef_x(b.cpb, ix, nx, cpml) * zx[i] + coef_x(b.cpa, ix, nx, cpml) * (p2 + tx) : 0.f;
-            if (xl) zx[i] = zxn;
-            G = p2 + (tx + zxn);
-        }
-        {
-            const bool zl = iz > nz - cpml - 1;
-            const float tz = iz > nz - cpml - 1 - kRad ? d1_strided(psz, i, pitch) * b.inv_dh : 0.f;
-            const float zzn = zl ? coef_z(b.cpb, iz, nz, cpml) * zz[i] + coef_z(b.cpa, iz, nz, cpml) * (r2 + tz) : 0.f;
-            if (zl) zz[i] = zzn;
-            H = r2 + (tz + zzn);
-        }
-        const long mi = (long)iz * b.mpitch + sh.x0 + ix;
-        const float mpH = b.mp[mi] * H;
-        float vp = Pv[i] + (b.mh[mi] * G + mpH);
-        float vf = Fv[i] + (b.mn[mi] * G + mpH);
-        if (ix == sh.sx && iz == sh.sz) { vp += w; vf += w; }
-        Pv[i] = vp;
-        Fv[i] = vf;
-        const float pn = P[i] + vp, fn = F[i] + vf;
-        Pn[i] = pn;
-        Fn[i] = fn;
-        if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1) b.rec[sh.rec_off + (long)it * nrec + (ix - sh.rx0)] = pn + fn;
-        if (img) {
-            img[i] = Cd::enc(EXACT ? G : p2, sc, b.status);
-            img[b.slot + i] = Cd::enc(EXACT ? H : r2, sc, b.status);
-        }
-        if (Cd::scaled) lmax = fmaxf(lmax, fmaxf(fabsf(pn), fabsf(fn)));
-    }
-    if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)s * (b.nt_max + 1) + g + 1]);
-}
-
-// Adjoint, the points the layer tiles left (after the strip pass and the layer tiles).
-// One thread per point loops over the active shots of its group in order
-// and adds their imaging to the group's gradient in one read-modify-write.
-//  EXACT: points within 4 of a layer, + Dxx(S ax Zx') - Dx(S ax Yx') (and the
-//         same along z) on scr[0] = Dxx U, scr[1] = Dzz V.
-//  reference: points inside the layers, the zeta recursion of
-//         src/parallelcalls.cu:216-243 on scr[0..3] = p2cx, r2dx, p2cz, r2cz.
-template <int ST, bool EXACT>
-__global__ void __launch_bounds__(kStripBlock) k_adj_cpml(Batch<float> b, int j, int ntb, int cur, int zsel,
-                                                          int img_base, int sg)
-{
-    using Cd = Codec<float, ST>;
-    const int grp = blockIdx.y;
-    const int s0 = grp * sg, s1 = min(s0 + sg, b.B);
-    const DevShot gsh = b.shots[s0];
-    const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
-    const StripMap smap = StripMap::make(nx, nz, EXACT ? cpml + kRad : cpml);
-    const int lag = EXACT ? 0 : 1;
-    const int img_g = ntb - 1 - lag - j;
-    using C = Coef<float>;
-    const float c2[5] = {C::d2_0, C::d2_1, -C::d2_2, C::d2_3, -C::d2_4};
-    const float c1[4] = {C::d1_1, -C::d1_2, C::d1_3, -C::d1_4};
-    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < smap.count();
-         k += (long)gridDim.x * blockDim.x) {
-        int ix, iz;
-        smap.point(k, ix, iz);
-        const long i = (long)iz * pitch + ix;
-        const bool xl = ix < cpml || ix > nx - cpml - 1, zl = iz > nz - cpml - 1;
-        const bool xn = ix < cpml + kRad || ix > nx - cpml - 1 - kRad, zn = iz > nz - cpml - 1 - kRad;
-        const float ax = coef_x(b.cpa, ix, nx, cpml), bx = coef_x(b.cpb, ix, nx, cpml);
-        const float az = coef_z(b.cpa, iz, nz, cpml), bz = coef_z(b.cpb, iz, nz, cpml);
-        float ah = 0.f, ap = 0.f, an = 0.f;
-        bool touched = false;
-        for (int s = s0; s < s1; s++) {
-            const DevShot sh = b.shots[s];
-            if (j >= sh.nt) continue;
-            touched = true;
-            const long so = (long)s * b.slot;
-            float ex, ez;
-            if (EXACT) {
-                ex = b.scr[0][so + i];
-                ez = b.scr[1][so + i];
-                if (xn) {
-                    const float *Zx = b.cp[3 - zsel] + so, *Yx = b.cp[0] + so;
-                    float a2 = c2[0] * ax * Zx[i], a1 = 0.f;
-#pragma unroll
-                    for (int q = 1; q <= 4; q++) {
-                        const float aP = coef_x(b.cpa, ix + q, nx, cpml), aM = coef_x(b.cpa, ix - q, nx, cpml);
-                        a2 += c2[q] * (aP * Zx[i + q] + aM * Zx[i - q]);
-                        a1 += c1[q - 1] * (aP * Yx[i + q] - aM * Yx[i - q]);
-                    }
-                    ex += a2 * b.inv_dh2 - a1 * b.inv_dh;
-                }
-                if (zn) {
-                    const float *Zz = b.cp[5 - zsel] + so, *Yz = b.cp[1] + so;
-                    float a2 = c2[0] * az * Zz[i], a1 = 0.f;
-#pragma unroll
-                    for (int q = 1; q <= 4; q++) {
-                        const long up = i + (long)q * pitch, dn = i - (long)q * pitch;
-                        const float aP = coef_z(b.cpa, iz + q, nz, cpml), aM = coef_z(b.cpa, iz - q, nz, cpml);
-                        a2 += c2[q] * (aP * Zz[up] + aM * Zz[dn]);
-                        a1 += c1[q - 1] * (aP * Yz[up] - aM * Yz[dn]);
-                    }
-                    ez += a2 * b.inv_dh2 - a1 * b.inv_dh;
-                }
-            } else {
-                const float p2cx = b.scr[0][so + i], r2dx = b.scr[1][so + i];
-                const float p2cz = b.scr[2][so + i], r2cz = b.scr[3][so + i];
-                const float *psixcx = b.cp[0] + so, *psixcz = b.cp[1] + so;
-                const float *psizdx = b.cp[2] + so, *psizcz = b.cp[3] + so;
-                float *zxcx = b.cp[4] + so, *zxcz = b.cp[5] + so, *zzdx = b.cp[6] + so, *zzcz = b.cp[7] + so;
-                float dxcx = 0.f, dzdx = 0.f, dxcz = 0.f, dzcz = 0.f;
-                if (xn) {
-                    dxcx = d1_strided(psixcx, i, 1) * b.inv_dh;
-                    dzdx = d1_strided(psizdx, i, 1) * b.inv_dh;
-                }
-                if (zn) {
-                    dxcz = d1_strided(psixcz, i, pitch) * b.inv_dh;
-                    dzcz = d1_strided(psizcz, i, pitch) * b.inv_dh;
-                }
-                float n1 = 0.f, n2 = 0.f, n3 = 0.f, n4 = 0.f;
-                if (xl) {
-                    n1 = bx * zxcx[i] + ax * (dxcx + p2cx);
-                    n3 = bx * zzdx[i] + ax * (dzdx + r2dx);
-                    zxcx[i] = n1;
-                    zzdx[i] = n3;
-                }
-                if (zl) {
-                    n2 = bz * zxcz[i] + az * (dxcz + p2cz);
-                    n4 = bz * zzcz[i] + az * (dzcz + r2cz);
-                    zxcz[i] = n2;
-                    zzcz[i] = n4;
-                }
-                ex = (p2cx + r2dx) + ((n1 + dxcx) + (n3 + dzdx));
-                ez = (p2cz + r2cz) + ((n2 + dxcz) + (n4 + dzcz));
-            }
-            const float *lP = b.lvl[cur] + so, *lF = b.lvl[2 + cur] + so;
-            float *lPw = b.lvl[4] + so, *lFw = b.lvl[5] + so;
-            float wp = lPw[i] + ex, wf = lFw[i] + ez;
-            const int mm = sh.nt - j;
-            if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1) {
-                const float d = b.rec[sh.rec_off + (long)(mm - 1) * (sh.rx1 - sh.rx0) + (ix - sh.rx0)];
-                wp += d;
-                wf += d;
-            }
-            lPw[i] = wp;
-            lFw[i] = wf;
-            const float pn = lP[i] + wp, fn = lF[i] + wf;
-            b.lvl[1 - cur][so + i] = pn;
-            b.lvl[3 - cur][so + i] = fn;
-            if (mm - 1 - lag >= 0) {
-                const typename Cd::S *img =
-                    (const typename Cd::S *)b.store + ((long)s * b.n_img + (img_g - img_base)) * 2 * b.slot;
-                const float inv_sc = Cd::scaled ? 1.f / b.scale[(long)s * b.nt_max + img_g] : 1.f;
-                const float kk = b.img_scale;
-                const float Gv = Cd::dec(img[i], inv_sc), Hv = Cd::dec(img[b.slot + i], inv_sc);
-                ah += kk * Gv * pn;
-                ap += kk * Hv * (pn + fn);
-                an += kk * Gv * fn;
-            }
-        }
-        if (touched) {
-            const long gi = (long)grp * b.slot + i;
-            b.g[0][gi] += ah;
-            b.g[1][gi] += ap;
-            b.g[2][gi] += an;
-        }
     }
 }
 
