@@ -501,12 +501,13 @@ template <typename T> struct Ctx : CtxBase {
     fwi::StepStreams ss{};  // st, plus the side streams of the FP32 step (prop_f32.cu)
 
 
-    // Interior points of the interior tiles of a window nxw wide (tile_role 1 for width aw).
-    long interior_tile_points(int nxw, int aw) const
+    // Interior points of the interior tiles of a window nxw wide (tile_role 1
+    // for width aw) on the tile grid from (xbase, zbase).
+    long interior_tile_points(int nxw, int aw, int xbase, int zbase) const
     {
         long n = 0;
-        for (int z0 = 0; z0 < nz; z0 += fwi::kTileEdge)
-            for (int x0 = 0; x0 < nxw; x0 += fwi::kTileEdge)
+        for (int z0 = zbase; z0 < nz; z0 += fwi::kTileEdge)
+            for (int x0 = xbase; x0 < nxw; x0 += fwi::kTileEdge)
                 if (fwi::tile_role(x0, z0, nxw, nz, aw) == 1) {
                     const long w = std::min(x0 + fwi::kTileEdge - 1, nxw - 5) - std::max(x0, 4) + 1;
                     const long h = std::min(z0 + fwi::kTileEdge - 1, nz - 5) - std::max(z0, 4) + 1;
@@ -691,6 +692,13 @@ template <typename T> struct Ctx : CtxBase {
     // group count gives about three waves of adjoint tile blocks (3 resident
     // per SM of a 152-SM GB300).  Measured on 601 x 301, 32 shots: 5 shots
     // per group (7 groups) 56.8 shots/s, 8: 53.8, 3: 52.3, 16: 40.6.
+    static bool uniform_windows(const std::vector<DevShot> &bs)
+    {
+        for (const DevShot &d : bs)
+            if (d.x0 != bs[0].x0 || d.nx != bs[0].nx) return false;
+        return true;
+    }
+
     int shots_per_group(const std::vector<DevShot> &bs, int nxm) const
     {
         if (!use_tma) return 1;
@@ -714,15 +722,15 @@ template <typename T> struct Ctx : CtxBase {
     // pass, without a block prologue per shot.  Measured on 601 x 301, 32
     // shots (54 layer tiles): 8 shots per group 60.2 shots/s, 5: 59.1,
     // 16: 54.9, 2: 56.6, 1: 53.4.
-    int layer_shots_per_group(int nb, int nxm) const
+    int layer_shots_per_group(int nb, int nxm, int xbase, int zbase) const
     {
         if (const char *e = getenv("FWI_LAYER_SHOTS_PER_GROUP")) {  // tuning override
             const int v = atoi(e);
             if (v >= 1) return std::min(v, 64);
         }
         long tiles = 0;
-        for (int z0 = 0; z0 < nz; z0 += fwi::kTileEdge)
-            for (int x0 = 0; x0 < nxm; x0 += fwi::kTileEdge)
+        for (int z0 = zbase; z0 < nz; z0 += fwi::kTileEdge)
+            for (int x0 = xbase; x0 < nxm; x0 += fwi::kTileEdge)
                 tiles += fwi::tile_role(x0, z0, nxm, nz, cfg.cpml + fwi::kRad) == 2;
         const long slots = 3L * 152 / 2;
         const long groups = std::max(1L, std::min((long)nb, (slots + tiles / 2) / std::max(1L, tiles)));
@@ -867,6 +875,8 @@ template <typename T> struct Ctx : CtxBase {
         b.status = status;
         b.sg = 1;
         b.sg_layer = 1;
+        b.xbase = b.zbase = 0;
+        b.inline_strip = 0;
         b.tma = use_tma ? (const void *)&maps : nullptr;
         return b;
     }
@@ -944,7 +954,15 @@ template <typename T> struct Ctx : CtxBase {
             TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
             Batch<T> b = batch_view(nb);
             b.sg = shots_per_group(bs, nxm);
-            b.sg_layer = b.sg == 1 ? 1 : layer_shots_per_group(nb, nxm);
+            if (use_tma && uniform_windows(bs)) {  // one tile grid fits every shot
+                const fwi::TileGrid tg = fwi::tile_grid(nxm, nz, cfg.cpml);
+                b.xbase = tg.xbase;
+                b.zbase = tg.zbase;
+                b.inline_strip = tg.inline_strip;
+                if (const char *e = getenv("FWI_INLINE_STRIP"))  // 0: the strip pass path (tests)
+                    if (atoi(e) == 0) b.inline_strip = 0;
+            }
+            b.sg_layer = b.sg == 1 ? 1 : layer_shots_per_group(nb, nxm, b.xbase, b.zbase);
             const int ngroups = (nb + b.sg - 1) / b.sg;
             // gradient slots in use: the interior groups' and the layer tiles' (same window in all)
             const int nslots = std::max(ngroups, (nb + b.sg_layer - 1) / b.sg_layer);
@@ -961,7 +979,8 @@ template <typename T> struct Ctx : CtxBase {
                 const int aw = phase == 0 || !exact ? cfg.cpml : cfg.cpml + fwi::kRad;
                 double pts = 0;
                 for (const DevShot &d : bs)
-                    if (phase == 0 ? step - (ntb - d.nt) >= 0 : step < d.nt) pts += (double)interior_tile_points(d.nx, aw);
+                    if (phase == 0 ? step - (ntb - d.nt) >= 0 : step < d.nt)
+                        pts += (double)interior_tile_points(d.nx, aw, b.xbase, b.zbase);
                 const int k = nsamp[phase]++;
                 spts[phase][k] = pts;
                 sst.t0 = tev[phase][k][0];

@@ -43,6 +43,8 @@ template <typename T> struct Batch {
                             // g[k] + q * slot accumulates the imaging of group q
     int sg_layer;           // the same for the FP32 layer tiles (their points are disjoint
                             // from the other passes', so the slots do not collide)
+    int xbase, zbase;       // FP32 tile grid origin (TileGrid)
+    int inline_strip;       // FP32: the layer tiles advance the CPML memory variables
     const void *tma;        // host copy of the batch's TMA tensor maps (FP32 path), or null
 };
 
@@ -67,6 +69,41 @@ constexpr int kTileEdge = 32;
 __host__ __device__ inline bool layer_point(int ix, int iz, int nx, int nz, int aw)
 {
     return ix < aw || ix > nx - aw - 1 || iz > nz - aw - 1;
+}
+
+// Tile grid origin of a window: tiles start at (xbase + 32 i, zbase + 32 j),
+// xbase, zbase in (-32, 0], xbase a multiple of 4 (TMA: the x coordinate of
+// every load, x0 - 4, stays a multiple of 16 bytes).  With `inline_strip`
+// the origin puts each CPML band together with the 4 points beside it (the
+// points whose updates read the band's memory variables) inside one tile
+// column (side bands) or row (bottom band); the layer tiles then advance
+// the memory variables themselves.  When no origin does that, both are 0.
+struct TileGrid {
+    int xbase = 0, zbase = 0;
+    bool inline_strip = false;
+};
+
+__host__ __device__ inline int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+inline TileGrid tile_grid(int nx, int nz, int cpml)
+{
+    TileGrid t;
+    const int w = cpml + 4;  // band plus the points beside it
+    if (cpml < 5 || w > kTileEdge || nx < 2 * w + 8 || nz < w + 8) return t;
+    auto same_tile = [](int a, int b, int base) {
+        return floor_div(a - base, kTileEdge) == floor_div(b - base, kTileEdge);
+    };
+    for (int xb = 0; xb > -kTileEdge; xb -= 4) {
+        if (!same_tile(4, w - 1, xb) || !same_tile(nx - w, nx - 5, xb)) continue;
+        for (int zb = 0; zb > -kTileEdge; zb--) {
+            if (!same_tile(nz - w, nz - 5, zb)) continue;
+            t.xbase = xb;
+            t.zbase = zb;
+            t.inline_strip = true;
+            return t;
+        }
+    }
+    return t;
 }
 
 // Role of the tile at (x0, z0) of an nx x nz window: 0 no interior point,

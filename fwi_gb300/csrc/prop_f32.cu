@@ -1,10 +1,11 @@
 // FP32 propagation, per step, on two streams (StepStreams):
-//   side stream (high priority): strip pass (prop.cuh: the CPML memory
-//                 variables) -> layer tiles (prop_layer.cuh)
+//   side stream (high priority): layer tiles (prop_layer.cuh), which advance
+//                 the CPML memory variables themselves when the tile grid
+//                 allows (TileGrid::inline_strip), else after the strip
+//                 pass of prop.cuh
 //   main stream:  interior tiles (prop_tma.cuh)
 // joined before the next step.  Both tile passes read only the current time
-// level and write disjoint points; the layer tiles read the memory variables
-// the strip pass just advanced.  The generic passes of prop.cuh serve FP64.
+// level and write disjoint points.  The generic passes of prop.cuh serve FP64.
 #include "prop_layer.cuh"
 
 namespace fwi {
@@ -16,9 +17,10 @@ template <typename K> void allow_smem(K kernel, size_t bytes)
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// Tiles from the grid origin (b.xbase, b.zbase) to the window's far edges.
 inline dim3 tma_grid(const Batch<float> &b, int nx_max, int sg)
 {
-    return dim3((nx_max + TT - 1) / TT, (b.nz + TT - 1) / TT, (b.B + sg - 1) / sg);
+    return dim3((nx_max - b.xbase + TT - 1) / TT, (b.nz - b.zbase + TT - 1) / TT, (b.B + sg - 1) / sg);
 }
 
 template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
@@ -30,13 +32,13 @@ template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, in
                                                                        ntb, cur, slot, b.sg);
 }
 
-template <int ST, bool EXACT>
+template <int ST, bool EXACT, bool INLINE>
 void fwd_layer(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
 {
     static bool set = false;
     const size_t sm = fwd_layer_smem();
-    if (!set) { allow_smem(k_fwd_layer<ST, EXACT>, sm); set = true; }
-    k_fwd_layer<ST, EXACT><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
+    if (!set) { allow_smem(k_fwd_layer<ST, EXACT, INLINE>, sm); set = true; }
+    k_fwd_layer<ST, EXACT, INLINE><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
         b, *static_cast<const TmaMaps *>(b.tma), g, ntb, cur, slot, b.sg_layer);
 }
 
@@ -50,13 +52,13 @@ void adj_interior(const Batch<float> &b, int nx_max, int j, int ntb, int cur, in
         b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, base, b.sg);
 }
 
-template <int ST, bool EXACT>
+template <int ST, bool EXACT, bool INLINE>
 void adj_layer(const Batch<float> &b, int nx_max, int j, int ntb, int cur, int zsel, int base, cudaStream_t st)
 {
     static bool set = false;
     const size_t sm = adj_layer_smem();
-    if (!set) { allow_smem(k_adj_layer<ST, EXACT>, sm); set = true; }
-    k_adj_layer<ST, EXACT><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
+    if (!set) { allow_smem(k_adj_layer<ST, EXACT, INLINE>, sm); set = true; }
+    k_adj_layer<ST, EXACT, INLINE><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
         b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, base, b.sg_layer);
 }
 
@@ -87,9 +89,14 @@ void forward_step(const Batch<float> &b, int nx_max, int g, int ntb, int cur, in
     fork_join(
         ss,
         [&](cudaStream_t s) {
+            if (b.inline_strip) {
+                if (exact) fwd_layer<ST, true, true>(b, nx_max, g, ntb, cur, slot, s);
+                else fwd_layer<ST, false, true>(b, nx_max, g, ntb, cur, slot, s);
+                return;
+            }
             k_fwd_strip<float><<<strip_grid(b, nx_max), kStripBlock, 0, s>>>(b, g, ntb, cur);
-            if (exact) fwd_layer<ST, true>(b, nx_max, g, ntb, cur, slot, s);
-            else fwd_layer<ST, false>(b, nx_max, g, ntb, cur, slot, s);
+            if (exact) fwd_layer<ST, true, false>(b, nx_max, g, ntb, cur, slot, s);
+            else fwd_layer<ST, false, false>(b, nx_max, g, ntb, cur, slot, s);
         },
         [&](cudaStream_t s) { fwd_interior<ST>(b, nx_max, g, ntb, cur, slot, s); });
 }
@@ -101,12 +108,17 @@ void adjoint_step(const Batch<float> &b, int nx_max, int j, int ntb, int cur, in
     fork_join(
         ss,
         [&](cudaStream_t s) {
+            if (b.inline_strip) {
+                if (exact) adj_layer<ST, true, true>(b, nx_max, j, ntb, cur, zsel, base, s);
+                else adj_layer<ST, false, true>(b, nx_max, j, ntb, cur, zsel, base, s);
+                return;
+            }
             if (exact) {
                 k_adj_strip_exact<float><<<strip_grid(b, nx_max), kStripBlock, 0, s>>>(b, j, cur, zsel);
-                adj_layer<ST, true>(b, nx_max, j, ntb, cur, zsel, base, s);
+                adj_layer<ST, true, false>(b, nx_max, j, ntb, cur, zsel, base, s);
             } else {
                 k_adj_strip_ref<float><<<strip_grid(b, nx_max), kStripBlock, 0, s>>>(b, j, cur);
-                adj_layer<ST, false>(b, nx_max, j, ntb, cur, zsel, base, s);
+                adj_layer<ST, false, false>(b, nx_max, j, ntb, cur, zsel, base, s);
             }
         },
         [&](cudaStream_t s) {

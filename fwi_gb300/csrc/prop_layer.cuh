@@ -62,12 +62,14 @@ __device__ __forceinline__ void row12(const float *row, float *v)
 
 // ------------------------------------------------------------------ forward
 
-// Forward layer tiles (src/parallelcalls.cu:65-117 at the strip points):
+// Forward layer tiles (src/parallelcalls.cu:48-117 at the strip points):
 // G = Dxx P + (Dx psi_x + zeta_x'), zeta_x' = b zeta_x + a (Dxx P + Dx psi_x)
 // (and H along z), only at strip points; the other points of the tile as
 // in the interior.  EXACT stores images of G, H; the reference's of the
-// plain stencils.
-template <int ST, bool EXACT>
+// plain stencils.  INLINE (TileGrid::inline_strip): the tile advances psi
+// of its own band points, psi = b psi + a Dx P, from the staged P and F
+// instead of loading what the strip pass wrote.
+template <int ST, bool EXACT, bool INLINE>
 __global__ void __launch_bounds__(kTmaThreads, 2)
 k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, int cur, int img_slot, int sg)
 {
@@ -78,7 +80,7 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
     __shared__ int act[kMaxGroup];
     __shared__ FwdShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
+    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
     const DevShot gsh = b.shots[blockIdx.z * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
     if (tile_role(x0, z0, nx, nz, cpml) != 2) return;
@@ -88,6 +90,11 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
         for (int k = 0; k < kLayerStages; k++) mbar_init(&bar[k], 1);
         mbar_init_fence();
     }
+    if (INLINE)  // psi tiles are computed here: their halos stay zero
+        for (int k = 0; k < kLayerStages; k++) {
+            float *sx = &stage[k].SX[0][0], *szp = &stage[k].SZ[0][0];
+            for (int i = tid; i < TT * TH; i += kTmaThreads) sx[i] = szp[i] = 0.f;
+        }
     if (tid < na) {
         const int s = act[tid];
         const DevShot sh = b.shots[s];
@@ -110,11 +117,13 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
         const int s = act[a];
         FwdLayerStage &S = stage[a % kLayerStages];
         uint64_t *br = &bar[a % kLayerStages];
-        mbar_expect_tx(br, (unsigned)sizeof(FwdLayerStage));
+        mbar_expect_tx(br, (unsigned)(INLINE ? sizeof(S.P) + sizeof(S.F) : sizeof(FwdLayerStage)));
         tma_load_3d(S.P, &maps.px[cur], br, x0 - kRad, z0, s);
         tma_load_3d(S.F, &maps.fz[cur], br, x0, z0 - kRad, s);
-        tma_load_3d(S.SX, &maps.mx[0], br, x0 - kRad, z0, s);
-        tma_load_3d(S.SZ, &maps.mz[1], br, x0, z0 - kRad, s);
+        if (!INLINE) {
+            tma_load_3d(S.SX, &maps.mx[0], br, x0 - kRad, z0, s);
+            tma_load_3d(S.SZ, &maps.mz[1], br, x0, z0 - kRad, s);
+        }
     };
     if (tid == 0)
         for (int k = 0; k < min(kLayerStages, na); k++) issue(k);
@@ -144,25 +153,50 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
     const long ipt = (long)iz * pitch + ix0;
     float *const Pn0 = b.lvl[1 - cur], *const Fn0 = b.lvl[3 - cur];
     float *const Pv0 = b.lvl[4], *const Fv0 = b.lvl[5];
-    float *const zx0 = b.cp[2], *const zz0 = b.cp[3];
+    float *const psx0 = b.cp[0], *const psz0 = b.cp[1], *const zx0 = b.cp[2], *const zz0 = b.cp[3];
     for (int a = 0; a < na; a++) {
         const FwdShot &sh = ps[a];
         const long so = sh.so;
-        float4 vP = make_float4(0.f, 0.f, 0.f, 0.f), vF = vP, zX = vP, zZ = vP;
+        float4 vP = make_float4(0.f, 0.f, 0.f, 0.f), vF = vP, zX = vP, zZ = vP, pX = vP, pZ = vP;
         if (any) {  // own points: issued before the wait
             vP = ld4(Pv0 + so + ipt);
             vF = ld4(Fv0 + so + ipt);
             if (anyS) {
                 zX = ld4(zx0 + so + ipt);
                 zZ = ld4(zz0 + so + ipt);
+                if (INLINE) {
+                    pX = ld4(psx0 + so + ipt);
+                    pZ = ld4(psz0 + so + ipt);
+                }
             }
         }
         if (!stage_ready(&bar[a % kLayerStages], (a / kLayerStages) & 1, b.status)) {
             drain_stages_n(bar, a, na, kLayerStages);
             return;
         }
-        const FwdLayerStage &S = stage[a % kLayerStages];
+        FwdLayerStage &S = stage[a % kLayerStages];
         float lmax = 0.f;
+        if (INLINE) {
+            // psi of the own band points (src/parallelcalls.cu:48-63); other cells stay 0
+            if (any && anyS) {
+                float pv[12];
+                row12(&S.P[r][c4], pv);
+                float4 fz[9];
+#pragma unroll
+                for (int k = 0; k < 9; k++) fz[k] = ld4(&S.F[r + k][c4]);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    float px = 0.f, pz = 0.f;
+                    if (xl[q]) px = bx[q] * comp(pX, q) + ax[q] * (d1_row(pv, q) * b.inv_dh);
+                    if (S4[q] && zl) pz = bz * comp(pZ, q) + az * (d1_col(fz, q) * b.inv_dh);
+                    S.SX[r][c4 + kRad + q] = px;
+                    S.SZ[r + kRad][c4 + q] = pz;
+                    if (xl[q]) psx0[so + ipt + q] = px;
+                    if (S4[q] && zl) psz0[so + ipt + q] = pz;
+                }
+            }
+            __syncthreads();  // the tile's psi complete
+        }
         if (any) {
             float pv[12];
             row12(&S.P[r][c4], pv);
@@ -279,7 +313,11 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
 //  reference: at strip points, the four second derivatives of the
 //         model-weighted fields and the zeta recursion of
 //         src/parallelcalls.cu:200-243 on the psi of this step's strip pass.
-template <int ST, bool EXACT>
+// INLINE (TileGrid::inline_strip): the tile advances the memory variables
+// of its own band points itself (what the strip pass would), from the
+// staged fields and, for the exact adjoint, the previous Z staged with its
+// halo: Zx' = g + bx Zx, Yx' = -Dx[S (g + ax (g + bx Zx))] + bx Yx (and z).
+template <int ST, bool EXACT, bool INLINE>
 __global__ void __launch_bounds__(kTmaThreads, 2)
 k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int zsel, int img_base,
             int sg)
@@ -295,11 +333,13 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
     float(*MP)[TT] = reinterpret_cast<float(*)[TT]>(MN + TT);                                    // [TH][TT]
     float(*U)[TH] = reinterpret_cast<float(*)[TH]>(MP + TH);                                     // [TT][TH]
     float(*V)[TT] = reinterpret_cast<float(*)[TT]>(U + TT);                                      // [TH][TT]
+    float(*WX)[TH] = reinterpret_cast<float(*)[TH]>(V + TH);  // [TT][TH] INLINE exact: S (g + ax Zx')
+    float(*WZ)[TT] = reinterpret_cast<float(*)[TT]>(WX + TT);  // [TH][TT]
     __shared__ __align__(8) uint64_t bar[kLayerStages];
     __shared__ int act[kMaxGroup];
     __shared__ AdjShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
+    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
     const int grp = blockIdx.z;
     const DevShot gsh = b.shots[grp * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
@@ -312,6 +352,18 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
     if (tid == 0) {
         for (int k = 0; k < kLayerStages; k++) mbar_init(&bar[k], 1);
         mbar_init_fence();
+    }
+    if (INLINE) {  // arrays computed here (not loaded): their halos stay zero
+        for (int k = 0; k < kLayerStages; k++) {
+            float *pb = &stage[k].B[0][0], *pd = &stage[k].D[0][0];
+            float *pa = &stage[k].A[0][0], *pc = &stage[k].C[0][0];
+            for (int i = tid; i < TT * TH; i += kTmaThreads) {
+                pb[i] = pd[i] = 0.f;
+                if (!EXACT) pa[i] = pc[i] = 0.f;
+            }
+        }
+        float *wx = &WX[0][0], *wz = &WZ[0][0];
+        for (int i = tid; i < TT * TH; i += kTmaThreads) wx[i] = wz[i] = 0.f;
     }
     if (tid < na) {
         const int s = act[tid];
@@ -330,24 +382,37 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
     // EXACT: A = Zx', B = Yx, C = Zz', D = Yz;  reference: A = psi_xcx, B = psi_zdx, C = psi_xcz, D = psi_zcz
     const CUtensorMap *mA = &maps.mx[EXACT ? 3 - zsel : 0], *mB = &maps.mx[EXACT ? 0 : 2];
     const CUtensorMap *mC = &maps.mz[EXACT ? 5 - zsel : 1], *mD = &maps.mz[EXACT ? 1 : 3];
+    // INLINE exact: A = Zx (old half), C = Zz (old half) staged; B = Yx', D = Yz' computed.
+    // INLINE reference: A..D computed.
+    if (INLINE && EXACT) {
+        mA = &maps.mx[2 + zsel];
+        mC = &maps.mz[4 + zsel];
+    }
     auto issue = [&](int a) {
         const int s = act[a];
         AdjLayerStage &S = stage[a % kLayerStages];
         uint64_t *br = &bar[a % kLayerStages];
-        mbar_expect_tx(br, (unsigned)sizeof(AdjLayerStage));
+        const unsigned bytes = !INLINE ? (unsigned)sizeof(AdjLayerStage)
+                               : EXACT ? (unsigned)(sizeof(S.P) + sizeof(S.F) + sizeof(S.A) + sizeof(S.C))
+                                       : (unsigned)(sizeof(S.P) + sizeof(S.F));
+        mbar_expect_tx(br, bytes);
         tma_load_3d(S.P, &maps.lvl[cur], br, x0 - kRad, z0 - kRad, s);
         tma_load_3d(S.F, &maps.lvl[2 + cur], br, x0 - kRad, z0 - kRad, s);
-        tma_load_3d(S.A, mA, br, x0 - kRad, z0, s);
-        tma_load_3d(S.B, mB, br, x0 - kRad, z0, s);
-        tma_load_3d(S.C, mC, br, x0, z0 - kRad, s);
-        tma_load_3d(S.D, mD, br, x0, z0 - kRad, s);
+        if (!INLINE || EXACT) {
+            tma_load_3d(S.A, mA, br, x0 - kRad, z0, s);
+            tma_load_3d(S.C, mC, br, x0, z0 - kRad, s);
+        }
+        if (!INLINE) {
+            tma_load_3d(S.B, mB, br, x0 - kRad, z0, s);
+            tma_load_3d(S.D, mD, br, x0, z0 - kRad, s);
+        }
     };
     if (tid == 0)
         for (int k = 0; k < min(kLayerStages, na); k++) issue(k);
     for (int k = tid; k < TT * TH; k += kTmaThreads) {
         const int rr = k / TH, cc = k - rr * TH;
         const int gx = x0 - kRad + cc, gz = z0 + rr;
-        const bool in = gx >= 0 && gx < nx && gz < nz;
+        const bool in = gx >= 0 && gx < nx && gz >= 0 && gz < nz;
         const long mi = (long)gz * b.mpitch + gsh.x0 + gx;
         MH[rr][cc] = in ? b.mh[mi] : 0.f;
         MN[rr][cc] = in ? b.mn[mi] : 0.f;
@@ -401,6 +466,7 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
     for (int a = 0; a < na; a++) {
         float4 wP = make_float4(0.f, 0.f, 0.f, 0.f), wF = wP;
         float4 zt[4] = {wP, wP, wP, wP};  // reference zeta: xcx, xcz, zdx, zcz
+        float4 yo[4] = {wP, wP, wP, wP};  // INLINE: old memory variables at the own points
         SI iG[4], iH[4];
         if (any) {
             const long so = ps[a].so;
@@ -413,12 +479,14 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
             }
             if (!EXACT && anyS)
                 for (int k = 0; k < 4; k++) zt[k] = ld4(b.cp[4 + k] + so + ipt);
+            if (INLINE && anyS)  // EXACT: Yx, Yz; reference: the four psi (updated in place)
+                for (int k = 0; k < (EXACT ? 2 : 4); k++) yo[k] = ld4(b.cp[k] + so + ipt);
         }
         if (!stage_ready(&bar[a % kLayerStages], (a / kLayerStages) & 1, b.status)) {
             drain_stages_n(bar, a, na, kLayerStages);
             return;
         }
-        const AdjLayerStage &S = stage[a % kLayerStages];
+        AdjLayerStage &S = stage[a % kLayerStages];
         for (int k = tid; k < TT * (TH / 4); k += kTmaThreads) {
             const int rr = k / (TH / 4), cc = 4 * (k - rr * (TH / 4));
             const float4 p = ld4(&S.P[rr + kRad][cc]), f = ld4(&S.F[rr + kRad][cc]);
@@ -435,6 +503,86 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
         __syncthreads();
         const AdjShot &sh = ps[a];
         const long so = sh.so;
+        if (INLINE) {
+            // the memory variables of the own band points, what the strip pass would
+            // compute (exact: this file's comment; reference: src/parallelcalls.cu:179-198)
+            if (any && anyS) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int ix = ix0 + q, c = c4 + q;
+                    const bool xl = S4[q] && (ix < cpml || ix > nx - cpml - 1);
+                    const bool zl = S4[q] && iz > nz - cpml - 1;
+                    const float axq = axw[4 + q], bxq_ = bxq[q], az = azw[4], bz = bzr;
+                    const long i = so + ipt + q;
+                    if (EXACT) {
+                        const float gq = U[r][c + kRad], hq = V[r + kRad][c];
+                        const float zxo = S.A[r][c + kRad], zzo = S.C[r + kRad][c];
+                        WX[r][c + kRad] = S4[q] ? gq + axq * (gq + bxq_ * zxo) : 0.f;
+                        WZ[r + kRad][c] = S4[q] ? hq + az * (hq + bz * zzo) : 0.f;
+                        const float zxn = xl ? gq + bxq_ * zxo : 0.f, zzn = zl ? hq + bz * zzo : 0.f;
+                        S.A[r][c + kRad] = zxn;  // own cell: Z' replaces the old Z
+                        S.C[r + kRad][c] = zzn;
+                        if (xl) b.cp[3 - zsel][i] = zxn;
+                        if (zl) b.cp[5 - zsel][i] = zzn;
+                    } else {
+                        float d1 = 0.f, d3 = 0.f, d2 = 0.f, d4 = 0.f;
+#pragma unroll
+                        for (int k = 1; k <= 4; k++) {
+                            d1 += c1[k - 1] * (MH[r][c + kRad + k] * S.P[r + kRad][c + kRad + k] -
+                                               MH[r][c + kRad - k] * S.P[r + kRad][c + kRad - k]);
+                            d3 += c1[k - 1] * (MN[r][c + kRad + k] * S.F[r + kRad][c + kRad + k] -
+                                               MN[r][c + kRad - k] * S.F[r + kRad][c + kRad - k]);
+                            d2 += c1[k - 1] * (MP[r + kRad + k][c] * S.P[r + kRad + k][c + kRad] -
+                                               MP[r + kRad - k][c] * S.P[r + kRad - k][c + kRad]);
+                            d4 += c1[k - 1] * (MP[r + kRad + k][c] * S.F[r + kRad + k][c + kRad] -
+                                               MP[r + kRad - k][c] * S.F[r + kRad - k][c + kRad]);
+                        }
+                        const float pxcx = xl ? bxq_ * comp(yo[0], q) + axq * (d1 * b.inv_dh) : 0.f;
+                        const float pzdx = xl ? bxq_ * comp(yo[2], q) + axq * (d3 * b.inv_dh) : 0.f;
+                        const float pxcz = zl ? bz * comp(yo[1], q) + az * (d2 * b.inv_dh) : 0.f;
+                        const float pzcz = zl ? bz * comp(yo[3], q) + az * (d4 * b.inv_dh) : 0.f;
+                        S.A[r][c + kRad] = pxcx;
+                        S.B[r][c + kRad] = pzdx;
+                        S.C[r + kRad][c] = pxcz;
+                        S.D[r + kRad][c] = pzcz;
+                        if (xl) {
+                            b.cp[0][i] = pxcx;
+                            b.cp[2][i] = pzdx;
+                        }
+                        if (zl) {
+                            b.cp[1][i] = pxcz;
+                            b.cp[3][i] = pzcz;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            if (EXACT) {
+                // Y' = -Dx W + b Y at the own band points (W complete now)
+                if (any && anyS) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int ix = ix0 + q, c = c4 + q;
+                        const bool xl = S4[q] && (ix < cpml || ix > nx - cpml - 1);
+                        const bool zl = S4[q] && iz > nz - cpml - 1;
+                        float ax_ = 0.f, az_ = 0.f;
+#pragma unroll
+                        for (int k = 1; k <= 4; k++) {
+                            ax_ += c1[k - 1] * (WX[r][c + kRad + k] - WX[r][c + kRad - k]);
+                            az_ += c1[k - 1] * (WZ[r + kRad + k][c] - WZ[r + kRad - k][c]);
+                        }
+                        const float yx = xl ? -ax_ * b.inv_dh + bxq[q] * comp(yo[0], q) : 0.f;
+                        const float yz = zl ? -az_ * b.inv_dh + bzr * comp(yo[1], q) : 0.f;
+                        S.B[r][c + kRad] = yx;
+                        S.D[r + kRad][c] = yz;
+                        const long i = so + ipt + q;
+                        if (xl) b.cp[0][i] = yx;
+                        if (zl) b.cp[1][i] = yz;
+                    }
+                }
+                __syncthreads();
+            }
+        }
         if (any) {
             float e0[4], e1[4];
             {
@@ -595,7 +743,8 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
 inline size_t fwd_layer_smem() { return 128 + kLayerStages * sizeof(FwdLayerStage); }
 inline size_t adj_layer_smem()
 {
-    return 128 + kLayerStages * sizeof(AdjLayerStage) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
+    return 128 + kLayerStages * sizeof(AdjLayerStage) +
+           sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT + TT * TH + TH * TT);
 }
 
 }  // namespace fwi

@@ -186,7 +186,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     __shared__ int act[kMaxGroup];
     __shared__ FwdShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
+    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
     const DevShot gsh = b.shots[blockIdx.z * sg];  // every shot of the group has this window
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
     if (tile_role(x0, z0, nx, nz, cpml) != 1) return;
@@ -377,7 +377,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     __shared__ int act[kMaxGroup];
     __shared__ AdjShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * TT, z0 = blockIdx.y * TT;
+    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
     const int grp = blockIdx.z;
     const DevShot gsh = b.shots[grp * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
@@ -419,7 +419,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     for (int k = tid; k < TT * TH; k += kTmaThreads) {
         const int rr = k / TH, cc = k - rr * TH;
         const int gx = x0 - kRad + cc, gz = z0 + rr;
-        const bool in = gx >= 0 && gx < nx && gz < nz;
+        const bool in = gx >= 0 && gx < nx && gz >= 0 && gz < nz;
         const long mi = (long)gz * b.mpitch + gsh.x0 + gx;
         MH[rr][cc] = in ? b.mh[mi] : 0.f;
         MN[rr][cc] = in ? b.mn[mi] : 0.f;
