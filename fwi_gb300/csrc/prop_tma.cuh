@@ -47,7 +47,8 @@ struct AdjStage {
     float F[TH][TH];
 };
 
-constexpr int kStages = 3;  // TMA pipeline depth over a group's shots
+constexpr int kStages = 3;     // TMA pipeline depth over a group's shots (forward interior tiles)
+constexpr int kAdjStages = 2;  // adjoint interior tiles: 2 stages keep 4 blocks on an SM
 
 __device__ __forceinline__ unsigned char *aligned_dsm(unsigned char *p)
 {
@@ -358,7 +359,7 @@ struct AdjShot {
 };
 
 template <int ST, bool EXACT>
-__global__ void __launch_bounds__(kTmaThreads, 3)
+__global__ void __launch_bounds__(kTmaThreads, 4)
 k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int zsel, int img_base,
           int sg)
 {
@@ -368,12 +369,12 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     extern __shared__ __align__(128) unsigned char dsm_raw[];
     unsigned char *dsm = aligned_dsm(dsm_raw);
     Stage *stage = reinterpret_cast<Stage *>(dsm);
-    float(*MH)[TH] = reinterpret_cast<float(*)[TH]>(dsm + kStages * sizeof(Stage));  // [TT][TH]
+    float(*MH)[TH] = reinterpret_cast<float(*)[TH]>(dsm + kAdjStages * sizeof(Stage));  // [TT][TH]
     float(*MN)[TH] = MH + TT;                                                          // [TT][TH]
     float(*MP)[TT] = reinterpret_cast<float(*)[TT]>(MN + TT);                          // [TH][TT]
     float(*U)[TH] = reinterpret_cast<float(*)[TH]>(MP + TH);                           // [TT][TH]
     float(*V)[TT] = reinterpret_cast<float(*)[TT]>(U + TT);                            // [TH][TT]
-    __shared__ __align__(8) uint64_t bar[kStages];
+    __shared__ __align__(8) uint64_t bar[kAdjStages];
     __shared__ int act[kMaxGroup];
     __shared__ AdjShot ps[kMaxGroup];
     const int tid = threadIdx.x;
@@ -388,7 +389,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     const int lag = EXACT ? 0 : 1;
     const int img_g = ntb - 1 - lag - j;  // global step of the image this iteration needs
     if (tid == 0) {
-        for (int k = 0; k < kStages; k++) mbar_init(&bar[k], 1);
+        for (int k = 0; k < kAdjStages; k++) mbar_init(&bar[k], 1);
         mbar_init_fence();
     }
     if (tid < na) {
@@ -407,14 +408,14 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     __syncthreads();
     auto issue = [&](int a) {
         const int s = act[a];
-        Stage &S = stage[a % kStages];
-        uint64_t *br = &bar[a % kStages];
+        Stage &S = stage[a % kAdjStages];
+        uint64_t *br = &bar[a % kAdjStages];
         mbar_expect_tx(br, (unsigned)sizeof(Stage));
         tma_load_3d(S.P, &maps.lvl[cur], br, x0 - kRad, z0 - kRad, s);
         tma_load_3d(S.F, &maps.lvl[2 + cur], br, x0 - kRad, z0 - kRad, s);
     };
     if (tid == 0)
-        for (int k = 0; k < min(kStages, na); k++) issue(k);
+        for (int k = 0; k < min(kAdjStages, na); k++) issue(k);
     // model tiles of the group's window: v_hor, v_nmo with the x-halo, v_po with the z-halo
     for (int k = tid; k < TT * TH; k += kTmaThreads) {
         const int rr = k / TH, cc = k - rr * TH;
@@ -459,11 +460,11 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                 Vec4Store<SI>::get(img + b.slot + ipt, iH);
             }
         }
-        if (!stage_ready(&bar[a % kStages], (a / kStages) & 1, b.status)) {
-            drain_stages(bar, a, na);
+        if (!stage_ready(&bar[a % kAdjStages], (a / kAdjStages) & 1, b.status)) {
+            drain_stages_n(bar, a, na, kAdjStages);
             return;
         }
-        const Stage &S = stage[a % kStages];
+        const Stage &S = stage[a % kAdjStages];
         // U = dt^2 (v_hor lP + v_nmo lF) on the x-halo tile, V = dt^2 v_po (lP + lF) on the z-halo tile
         for (int k = tid; k < TT * (TH / 4); k += kTmaThreads) {
             const int rr = k / (TH / 4), cc = 4 * (k - rr * (TH / 4));
@@ -545,9 +546,9 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
             }
         }
         __syncthreads();  // stage, U and V are free again
-        if (tid == 0 && a + kStages < na) {
+        if (tid == 0 && a + kAdjStages < na) {
             fence_proxy_async();
-            issue(a + kStages);
+            issue(a + kAdjStages);
         }
     }
     if (!any) return;
@@ -573,7 +574,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
 inline size_t fwd_tma_smem() { return 128 + kStages * sizeof(FwdStage); }
 inline size_t adj_tma_smem()
 {
-    return 128 + kStages * sizeof(AdjStage) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
+    return 128 + kAdjStages * sizeof(AdjStage) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
 }
 
 }  // namespace fwi
