@@ -369,6 +369,20 @@ __global__ void k_first_update(T *vh, T *vp, T *vn, const T *gh, const T *gp, co
     }
 }
 
+// Directional derivative of the misfit along the trial step m_back - alpha r:
+// out[p] = sum of g_p r_p over the rows the update changes (iz > kLayer), FP64.
+template <typename T>
+__global__ void k_lb_slope(CTri<T> g, CTri<T> r, int nx, int nz, int mpitch, DotScratch ds, double *out)
+{
+    double v[4][3] = {};
+    const long n = (long)nx * (nz - kLayer - 1);
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const long iz = kLayer + 1 + k / nx, ix = k % nx, i = iz * mpitch + ix;
+        for (int p = 0; p < 3; p++) v[0][p] += (double)g.p[p][i] * r.p[p][i];
+    }
+    reduce_last_block(v, 1, ds, out);
+}
+
 // Trial model (src/parallelcalls.cu:343-404) for all three parameters.
 template <typename T>
 __global__ void k_lb_update(T *vh, T *vp, T *vn, const T *bh, const T *bp, const T *bn, const T *rh,
@@ -475,6 +489,7 @@ struct CtxBase {
     virtual int first_step(float, float, float) = 0;
     virtual int lbfgs_direction(int, double *) = 0;
     virtual int lbfgs_update(float, float, float, int, int) = 0;
+    virtual int direction_slope(double *) = 0;
     virtual int restore_model() = 0;
     virtual int gradient_vti(void *, void *, void *) = 0;
     virtual int set_gradient(const void *, const void *, const void *) = 0;
@@ -547,6 +562,7 @@ template <typename T> struct Ctx : CtxBase {
     T *hs[kMaxHist][3] = {}, *hy[kMaxHist][3] = {};
     int hist_m = 0, hist_count = 0, hist_next = 0;
     bool have_back = false;
+    bool have_dir = false;  // r holds an L-BFGS direction from (mb, gb)
     LbScalars *lbs = nullptr;
     DotScratch ds{};
     T *vti_out[3] = {};
@@ -1215,6 +1231,7 @@ template <typename T> struct Ctx : CtxBase {
         TRY_LAUNCH();
         // the model and gradient this direction starts from (src/main.c:683-688)
         if ((rc = copy3(mb, m3)) || (rc = copy3(gb, grad))) return rc;
+        have_dir = true;
         if (stats) {
             LbScalars h;
             TRY(cudaMemcpyAsync(&h, lbs, sizeof(h), cudaMemcpyDeviceToHost, st));
@@ -1227,6 +1244,19 @@ template <typename T> struct Ctx : CtxBase {
             }
         }
         TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    int direction_slope(double *out3) override
+    {
+        if (!have_dir) return FWI_ERR_STATE;
+        k_lb_slope<T><<<kRedBlocks, kRedThreads, 0, st>>>(ctri(gb), ctri(r), nx, nz, mpitch, ds, lbs->dots);
+        TRY_LAUNCH();
+        launches++;
+        double d[3];
+        TRY(cudaMemcpyAsync(d, lbs->dots, sizeof(d), cudaMemcpyDeviceToHost, st));
+        TRY(cudaStreamSynchronize(st));
+        for (int p = 0; p < 3; p++) out3[p] = d[p];
         return FWI_OK;
     }
 
@@ -1420,6 +1450,18 @@ int fwi_first_step(void *ctx, float a, float b, float c) { return ctx ? as_ctx(c
 int fwi_lbfgs_direction(void *ctx, int m, double *stats)
 {
     return ctx ? as_ctx(ctx)->lbfgs_direction(m, stats) : FWI_ERR_ARG;
+}
+int fwi_get_config(void *ctx, fwi_config *out)
+{
+    if (!ctx || !out) return FWI_ERR_ARG;
+    *out = as_ctx(ctx)->cfg;
+    return FWI_OK;
+}
+
+int fwi_direction_slope(void *ctx, double *out3)
+{
+    if (!ctx || !out3) return FWI_ERR_ARG;
+    return as_ctx(ctx)->direction_slope(out3);
 }
 int fwi_lbfgs_update(void *ctx, float av, float ad, float ae, int fmin, int fmax)
 {

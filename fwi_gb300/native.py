@@ -56,7 +56,11 @@ class Config(C.Structure):
 class InvertOpts(C.Structure):
     _fields_ = [("iterations", C.c_int), ("lbfgs_m", C.c_int), ("first_alpha", C.c_float * 3),
                 ("alpha0", C.c_float), ("max_halvings", C.c_int), ("reset_alpha", C.c_int),
-                ("flag_min", C.c_int), ("flag_max", C.c_int)]
+                ("flag_min", C.c_int), ("flag_max", C.c_int), ("armijo_c1", C.c_double)]
+
+
+# int (*)(void *user, int band, float f, const void **obs)
+BandObsFn = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_float, C.POINTER(C.c_void_p))
 
 
 class Shot(C.Structure):
@@ -114,6 +118,11 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_residual_misfit_noalloc", [_p, _p, _p, _p, _l, _i, _p, _p])
         _sig(L, "fwi_invert_defaults", [C.POINTER(InvertOpts)], None)
         _sig(L, "fwi_invert", [_p, shotp, _i, _p, _p, C.POINTER(InvertOpts), _p, C.POINTER(_i)])
+        _sig(L, "fwi_invert_bands", [_p, shotp, _i, _p, _f, _f, _i, _i, BandObsFn, _p, C.POINTER(InvertOpts), _i,
+                                     _p, _p])
+        _sig(L, "fwi_direction_slope", [_p, _p])
+        _sig(L, "fwi_load_model_files", [_p, C.c_char_p, C.c_char_p, C.c_char_p])
+        _sig(L, "fwi_save_model_files", [_p, C.c_char_p, C.c_char_p, C.c_char_p])
         _sig(L, "fwi_set_frequency", [_p, _f, _i])
         # reference-compatible ABI: float* device pointers, ints, floats
         _sig(L, "pre_variables_h", [_p] * 6 + [_i, _i], None)
@@ -279,6 +288,52 @@ class Context:
         _check(lib().fwi_invert(self._h, shots, len(shots), ptr(obs), ptr(mask), C.byref(o),
                                 hist.ctypes.data, C.byref(done)), "fwi_invert")
         return hist[: done.value]
+
+    def invert_bands(self, shots, band_obs, f0, df, nbands, nt, mask=None, restart_model=False, **opts):
+        """Multiscale loop of the C driver; band_obs(band, f) returns that band's observed
+        data (host or device array).  Returns the misfits of each band."""
+        o = InvertOpts()
+        lib().fwi_invert_defaults(C.byref(o))
+        for k, v in opts.items():
+            if k == "first_alpha":
+                o.first_alpha[:] = list(v)
+            else:
+                setattr(o, k, v)
+        keep = []
+
+        def cb(user, band, f, out):
+            try:
+                d = band_obs(band, float(f))
+                if isinstance(d, np.ndarray):
+                    d = np.ascontiguousarray(d, self.dtype)
+                keep.append(d)
+                out[0] = C.c_void_p(ptr(d))
+                return 0
+            except Exception:  # noqa: BLE001 - reported to the driver as a failed band
+                return 1
+
+        fn = BandObsFn(cb)
+        if mask is not None:
+            mask = np.ascontiguousarray(mask, np.uint8)
+        hist = np.zeros(nbands * o.iterations, np.float64)
+        done = np.zeros(nbands, np.int32)
+        _check(lib().fwi_invert_bands(self._h, shots, len(shots), ptr(mask), float(f0), float(df), int(nbands),
+                                      int(nt), fn, None, C.byref(o), 1 if restart_model else 0,
+                                      hist.ctypes.data, done.ctypes.data), "fwi_invert_bands")
+        return [hist[b * o.iterations: b * o.iterations + done[b]] for b in range(nbands)]
+
+    def direction_slope(self):
+        out = np.zeros(3, np.float64)
+        _check(lib().fwi_direction_slope(self._h, out.ctypes.data), "fwi_direction_slope")
+        return out
+
+    def load_model_files(self, vp_path, eps_path, delta_path):
+        _check(lib().fwi_load_model_files(self._h, *(os.fsencode(p) for p in (vp_path, eps_path, delta_path))),
+               "fwi_load_model_files")
+
+    def save_model_files(self, vh_path, vp_path, vn_path):
+        _check(lib().fwi_save_model_files(self._h, *(os.fsencode(p) for p in (vh_path, vp_path, vn_path))),
+               "fwi_save_model_files")
 
     def set_ricker(self, f, nt):
         _check(lib().fwi_set_ricker(self._h, float(f), int(nt)), "fwi_set_ricker")

@@ -30,7 +30,7 @@ extern "C" {
 #define FWI_OK 0
 #define FWI_ERR_ARG (-1)       /* invalid argument or geometry */
 #define FWI_ERR_CUDA (-2)      /* a CUDA call failed (details: fwi_last_cuda_error) */
-#define FWI_ERR_NOMEM (-3)     /* device memory for the requested batch does not fit */
+#define FWI_ERR_NOMEM (-3)     /* device memory for the requested batch does not fit (or a host buffer) */
 #define FWI_ERR_STATE (-4)     /* call out of order (e.g. no model set) */
 #define FWI_ERR_NUMERIC (-5)   /* NaN/Inf met, or reduced-precision storage saturated */
 #define FWI_ERR_UNSUPPORTED (-6)
@@ -98,6 +98,9 @@ size_t fwi_config_bytes(const fwi_config *cfg);
 
 int fwi_create(const fwi_config *cfg, void **ctx_out);
 void fwi_destroy(void *ctx);
+
+/* The configuration a context was created with. */
+int fwi_get_config(void *ctx, fwi_config *out);
 const char *fwi_strerror(int status);
 /* The cudaError_t behind the last FWI_ERR_CUDA of this context (0 if none). */
 int fwi_last_cuda_error(void *ctx);
@@ -156,6 +159,12 @@ int fwi_lbfgs_update(void *ctx, float alpha_v, float alpha_d, float alpha_e, int
 /* Model back to m_back (src/main.c:777-784). */
 int fwi_restore_model(void *ctx);
 
+/* Directional derivative along the last L-BFGS direction r from (m_back, g_back):
+ * out[p] = sum over the rows fwi_lbfgs_update changes of g_back . r, FP64, order v_hor,
+ * v_po, v_nmo.  The trial m_back - alpha r changes the misfit by about -alpha sum(out).
+ * No counterpart in the reference (its line search compares misfits only). */
+int fwi_direction_slope(void *ctx, double *out3);
+
 /* ---- host driver (C) ----
  * One frequency band of the reference's inversion loop (src/main.c:396-801) over the calls
  * above: steepest first step, then L-BFGS directions with the backtracking line search
@@ -170,6 +179,8 @@ typedef struct {
     int max_halvings;     /* src/main.c:777: 5 */
     int reset_alpha;      /* 0: alpha and the halving count persist over the band, as the reference */
     int flag_min, flag_max; /* clamps of update_LBFGS (src/parallelcalls.cu:343-404) */
+    double armijo_c1;     /* 0: the reference's acceptance (trial misfit below the iteration's);
+                             > 0: also J_trial <= J - c1 alpha sum(fwi_direction_slope), FP64 */
 } fwi_invert_opts;
 
 void fwi_invert_defaults(fwi_invert_opts *opts);
@@ -180,6 +191,30 @@ int fwi_invert(void *ctx, const fwi_shot *shots, int nshots, const void *obs,
 /* Next frequency band (src/main.c:318-319, 328-333, 802): CPML profiles for peak
  * frequency f and a Ricker wavelet of nt samples at f. */
 int fwi_set_frequency(void *ctx, float f, int nt);
+
+/* Multiscale inversion (src/main.c:274-806): band b at peak frequency f0 + b df
+ * (the reference: f += 3).  Per band: fwi_set_frequency(f, nt); the band's observed data
+ * from band_obs (the caller's records, or its own forward modelling with
+ * fwi_forward), host or device, laid out as fwi_gradient takes them; then fwi_invert with
+ * alpha and the halving count starting afresh (src/main.c:308-311).  restart_model != 0
+ * starts every band from the model the call began with, as the reference does (it
+ * rebuilds the model from the initial Vp, eps, delta at src/main.c:318); 0 continues from
+ * the previous band.  misfit_history: nbands x opts->iterations (optional);
+ * iterations_done: nbands (optional). */
+typedef int (*fwi_band_obs_fn)(void *user, int band, float f, const void **obs);
+int fwi_invert_bands(void *ctx, const fwi_shot *shots, int nshots, const unsigned char *mask, float f0,
+                     float df, int nbands, int nt, fwi_band_obs_fn band_obs, void *user,
+                     const fwi_invert_opts *opts, int restart_model, double *misfit_history,
+                     int *iterations_done);
+
+/* ---- model files (src/main.c:101-123, 823-835) ----
+ * Raw float32 [nz][nx], x fastest, no header.  fwi_load_model_files reads Vp (m/s),
+ * epsilon and delta (the reference's vp_ori.bin, vh_ori.bin, vn_ori.bin) into the model
+ * (fwi_set_model_vti); fwi_save_model_files writes the squared velocities v_hor, v_po,
+ * v_nmo (the reference's vh_ini.bin, vp_ini.bin, vn_ini.bin).  FWI_ERR_ARG on a missing
+ * or short file. */
+int fwi_load_model_files(void *ctx, const char *vp_path, const char *eps_path, const char *delta_path);
+int fwi_save_model_files(void *ctx, const char *vh_path, const char *vp_path, const char *vn_path);
 
 /* Chain rule to the Vp / epsilon / delta parameterisation of the current model:
  * dJ/dVp = 2 Vp (g_po + (1 + 2 eps) g_hor + (1 + 2 delta) g_nmo),
