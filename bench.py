@@ -178,10 +178,13 @@ def native_arm(args, rank, world, dist):
     sprec = {"fp32": fwi_gb300.SPREC_NATIVE, "fp16": fwi_gb300.SPREC_FP16, "bf16": fwi_gb300.SPREC_BF16}[args.store]
     nrec = max(s["rx1"] - s["rx0"] for s in w.shots)
 
-    def context(max_shots, precision=fwi_gb300.PREC_FP32, store_prec=sprec):
+    storage = {"full": fwi_gb300.STORE_FULL, "checkpoint": fwi_gb300.STORE_CHECKPOINT,
+               "boundary": fwi_gb300.STORE_BOUNDARY}[args.storage]
+
+    def context(max_shots, precision=fwi_gb300.PREC_FP32, store_prec=sprec, store=storage):
         c = fwi_gb300.Context(nx=w.nx, nz=w.nz, dh=w.dh, dt=w.dt, cpml=w.cpml, f_cpml=w.f, nt_max=w.nt,
                               max_shots=max_shots, max_receivers=nrec, mode=mode, precision=precision,
-                              store_prec=store_prec, device=dev)
+                              store_prec=store_prec, store=store, device=dev)
         c.set_ricker(w.f, w.nt)
         return c
 
@@ -264,7 +267,7 @@ def native_arm(args, rank, world, dist):
             "data": "synthetic (seeded C2 model, observed data modelled on the GPU from the true model)",
             "config": {"workload": w.name, "nx": w.nx, "nz": w.nz, "dh": w.dh, "dt": w.dt, "nt": w.nt,
                        "shots": nshots, "receivers_per_shot": nrec, "ricker_hz": w.f, "cpml": w.cpml,
-                       "mode": args.mode, "image_store": f"full, {args.store}", "batch": args.batch,
+                       "mode": args.mode, "image_store": f"{args.storage}, {args.store}", "batch": args.batch,
                        "l2": "inputs larger than L2 (observed data 231 MB, images streamed through HBM)"},
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
@@ -296,7 +299,7 @@ def native_arm(args, rank, world, dist):
         # plain per-shot FP32 path (one shot per launch sequence, FP32 images), on a subset
         sub = fwi_gb300.make_shots(w.shots[: args.plain_shots])
         nsub = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots[: args.plain_shots])
-        c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE)
+        c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE, store=fwi_gb300.STORE_FULL)
         c1.set_model(*w.squared(initial=True))
         c1.gradient(sub, obs_d[:nsub])
         torch.cuda.synchronize()
@@ -310,7 +313,8 @@ def native_arm(args, rank, world, dist):
                             "how": f"max_shots=1, FP32 images, {args.plain_shots} shots timed",
                             "speedup": round(value / world / plain, 2)}
         # gradient error of this configuration against the FP64 GPU path, same shots
-        c64 = context(args.plain_shots, precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE)
+        c64 = context(args.plain_shots, precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE,
+                      store=fwi_gb300.STORE_FULL)
         c64.set_model(*(a.astype(np.float64) for a in w.squared(initial=True)))
         r64 = c64.gradient(sub, obs_d[:nsub].cpu().numpy().astype(np.float64))
         del c64
@@ -326,7 +330,7 @@ def native_arm(args, rank, world, dist):
             "misfit_rel_err": abs(rx[0] - r64[0]) / abs(r64[0])}
         # L-BFGS two-loop (m = 5) on this grid, FP64 dots
         from fwi_gb300 import Context
-        cl = context(1)
+        cl = context(1, store=fwi_gb300.STORE_FULL)
         cl.set_model(*w.squared(initial=True))
         cl.set_gradient(*(a.astype(np.float32) for a in r64[1:]))
         cl.first_step(3e5, 2e5, 2.5e5)
@@ -388,6 +392,8 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--mode", default="exact", choices=["exact", "ref"])
     ap.add_argument("--store", default="fp16", choices=["fp32", "fp16", "bf16"])
+    ap.add_argument("--storage", default="full", choices=["full", "checkpoint", "boundary"],
+                    help="how the forward images are kept (FWI_STORE_*)")
     ap.add_argument("--plain-shots", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")

@@ -7,4 +7,4 @@ package holds its build recipe (`fwi_gb300.build`), ctypes bindings
 """
 from .native import (Context, FwiError, Shot, lib, make_shots, ptr, strip_points,  # noqa: F401
                      MODE_EXACT, MODE_REF_COMPAT, PREC_FP32, PREC_FP64, SPREC_BF16,
-                     SPREC_FP16, SPREC_NATIVE, STORE_CHECKPOINT, STORE_FULL)
+                     SPREC_FP16, SPREC_NATIVE, STORE_BOUNDARY, STORE_CHECKPOINT, STORE_FULL)

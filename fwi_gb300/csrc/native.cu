@@ -541,6 +541,9 @@ template <typename T> struct Ctx : CtxBase {
     // batch
     T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {};
     void *store = nullptr;
+    // boundary storage: ring of every step [B][nt_max][ring_len], rebuild state in rlvl
+    T *ring = nullptr;
+    long ring_len = 0;
     // checkpointing: full states every ck_every steps, segment recompute buffers
     int ck_every = 0, n_ck = 0;
     T *ck = nullptr;                 // [n_ck][8][B * slot]: P, F, their increments, CPML x4
@@ -638,6 +641,12 @@ template <typename T> struct Ctx : CtxBase {
             TRY(alloc(&ck, (size_t)n_ck * 8 * B * slot));
             for (auto &p : rlvl) TRY(alloc(&p, (size_t)B * slot));
             for (auto &p : rcp) TRY(alloc(&p, (size_t)B * slot));
+        }
+        if (cfg.store == FWI_STORE_BOUNDARY) {
+            ring_len = fwi::boundary_ring_len(win, nz, cfg.cpml);
+            n_img = 1;  // the image of the step just rebuilt
+            TRY(alloc(&ring, (size_t)B * nt_max * ring_len));
+            for (auto &p : rlvl) TRY(alloc(&p, (size_t)B * slot));
         }
         {
             void *q0 = nullptr;
@@ -985,6 +994,7 @@ template <typename T> struct Ctx : CtxBase {
             cudaEvent_t e0 = ev[1], e1 = ev[2], e2 = ev[3];
             TRY(cudaEventRecord(e0, st));
             const bool ckpt = want_grad && cfg.store == FWI_STORE_CHECKPOINT;
+            const bool bnd = want_grad && cfg.store == FWI_STORE_BOUNDARY;
             // sampled steps of the interior tile timing: events and interior points updated
             const bool timed = tile_timing && sizeof(T) == 4;
             const int tstride = std::max(1, ntb / kTimeSamples);
@@ -1010,11 +1020,22 @@ template <typename T> struct Ctx : CtxBase {
                 }
                 fwi::StepStreams sst = ss;
                 sample(0, g, sst);
-                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt) ? g : -1, exact, sst);
+                if (bnd) fwi::launch_save_ring<T>(b, nxm, g, ntb, cur, ring, ring_len, st);
+                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt && !bnd) ? g : -1, exact, sst);
                 cur ^= 1;
             }
             TRY_LAUNCH();
-            launches += kps * ntb;
+            launches += (kps + (bnd ? 1 : 0)) * ntb;
+            if (bnd) {
+                // the final state (P, F, increments) starts the backward rebuild
+                for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+                TRY(cudaMemcpyAsync(rlvl[0], lvl[cur], lb, cudaMemcpyDeviceToDevice, st));
+                TRY(cudaMemcpyAsync(rlvl[2], lvl[2 + cur], lb, cudaMemcpyDeviceToDevice, st));
+                TRY(cudaMemcpyAsync(rlvl[4], lvl[4], lb, cudaMemcpyDeviceToDevice, st));
+                TRY(cudaMemcpyAsync(rlvl[5], lvl[5], lb, cudaMemcpyDeviceToDevice, st));
+                // images of the layer points stay zero
+                TRY(cudaMemsetAsync(store, 0, (size_t)nb * n_img * 2 * slot * store_elem(), st));
+            }
             TRY(cudaEventRecord(e1, st));
             if (obs_in) {
                 k_residual<T><<<dim3(kRedBlocks, nb), kRedThreads, 0, st>>>(rec, obs, mask_in ? mask : nullptr, shots,
@@ -1031,7 +1052,31 @@ template <typename T> struct Ctx : CtxBase {
                 for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
                 cur = 0;
                 int zsel = 0;
-                if (!ckpt) {
+                if (bnd) {
+                    // rebuild the CPML-free region backwards one step ahead of the adjoint
+                    // iteration that images it (image slot 0 holds the step just rebuilt)
+                    const int lag = exact ? 0 : 1;
+                    Batch<T> rb = b;
+                    for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
+                    fwi::launch_rebuild_begin<T>(rb, nxm, ntb - 1, ntb, 0, ring, ring_len, st);
+                    launches += 2;
+                    int rcur = 1, next_g = ntb - 1;
+                    for (int j = 0; j < ntb; j++) {
+                        const int need = ntb - 1 - lag - j;
+                        for (; next_g >= 0 && next_g >= need; next_g--) {
+                            fwi::launch_rebuild_step<T>(rb, nxm, next_g, ntb, rcur, ring, ring_len, st);
+                            rcur ^= 1;
+                            launches += 2;
+                        }
+                        fwi::StepStreams sst = ss;
+                        sample(1, j, sst);
+                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, need >= 0 ? need : 0, sst);
+                        cur ^= 1;
+                        zsel ^= 1;
+                        launches += kps;
+                    }
+                    TRY_LAUNCH();
+                } else if (!ckpt) {
                     for (int j = 0; j < ntb; j++) {
                         fwi::StepStreams sst = ss;
                         sample(1, j, sst);
@@ -1354,6 +1399,9 @@ size_t fwi_config_bytes(const fwi_config *c)
         const long k = checkpoint_interval(*c), n = (c->nt_max + k - 1) / k;
         b += (size_t)c->max_shots * slot * e * (8 * n + 10); // checkpoints, recompute state
         b += (size_t)c->max_shots * k * 2 * slot * se;       // images of one segment
+    } else if (c->store == FWI_STORE_BOUNDARY) {
+        b += (size_t)c->max_shots * c->nt_max * fwi::boundary_ring_len((int)win, c->nz, c->cpml) * e;  // rings
+        b += (size_t)c->max_shots * slot * (6 * e + 2 * se);  // rebuild state, one image
     } else {
         b += (size_t)c->max_shots * c->nt_max * 2 * slot * se; // images
     }
@@ -1369,7 +1417,9 @@ int fwi_create(const fwi_config *cfg, void **out)
         cfg->max_shots <= 0 || !(cfg->dh > 0) || !(cfg->dt > 0) || cfg->max_window < 0 || cfg->max_window > cfg->nx)
         return FWI_ERR_ARG;
     if (cfg->mode != FWI_MODE_EXACT && cfg->mode != FWI_MODE_REF_COMPAT) return FWI_ERR_ARG;
-    if (cfg->store != FWI_STORE_FULL && cfg->store != FWI_STORE_CHECKPOINT) return FWI_ERR_ARG;
+    if (cfg->store != FWI_STORE_FULL && cfg->store != FWI_STORE_CHECKPOINT && cfg->store != FWI_STORE_BOUNDARY)
+        return FWI_ERR_ARG;
+    if (cfg->store == FWI_STORE_BOUNDARY && cfg->cpml < 8) return FWI_ERR_UNSUPPORTED;  // ring inside the layers
     if (cfg->store_prec < FWI_SPREC_NATIVE || cfg->store_prec > FWI_SPREC_BF16) return FWI_ERR_ARG;
     if (cfg->precision == FWI_PREC_FP64 && cfg->store_prec != FWI_SPREC_NATIVE) return FWI_ERR_UNSUPPORTED;
     int ndev = 0;

@@ -145,4 +145,17 @@ template <typename T>
 void launch_adjoint_step(const Batch<T> &b, int nx_max, int j, int ntb, int cur, int zsel,
                          bool exact, int img_base, const StepStreams &ss);
 
+// Boundary storage (prop_boundary.cuh): ring length per shot, saving the
+// ring of step g, and the backward rebuild of the CPML-free region.
+long boundary_ring_len(int nx_max, int nz, int cpml);
+template <typename T>
+void launch_save_ring(const Batch<T> &b, int nx_max, int g, int ntb, int cur, T *ring, long ring_len,
+                      cudaStream_t st);
+template <typename T>
+void launch_rebuild_begin(const Batch<T> &rb, int nx_max, int g, int ntb, int src, const T *ring, long ring_len,
+                          cudaStream_t st);
+template <typename T>
+void launch_rebuild_step(const Batch<T> &rb, int nx_max, int g, int ntb, int cur, const T *ring, long ring_len,
+                         cudaStream_t st);
+
 }  // namespace fwi

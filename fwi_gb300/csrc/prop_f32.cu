@@ -6,6 +6,7 @@
 //   main stream:  interior tiles (prop_tma.cuh)
 // joined before the next step.  Both tile passes read only the current time
 // level and write disjoint points.  The generic passes of prop.cuh serve FP64.
+#include "prop_boundary.cuh"
 #include "prop_layer.cuh"
 
 namespace fwi {
@@ -150,5 +151,13 @@ void launch_adjoint_step<float>(const Batch<float> &b, int nx_max, int j, int nt
     default: adjoint_step<kStoreNative>(b, nx_max, j, ntb, cur, zsel, exact, img_base, ss); break;
     }
 }
+
+long boundary_ring_len(int nx_max, int nz, int cpml) { return Ring::make(nx_max, nz, cpml).count(); }
+
+template void launch_save_ring<float>(const Batch<float> &, int, int, int, int, float *, long, cudaStream_t);
+template void launch_rebuild_begin<float>(const Batch<float> &, int, int, int, int, const float *, long,
+                                          cudaStream_t);
+template void launch_rebuild_step<float>(const Batch<float> &, int, int, int, int, const float *, long,
+                                         cudaStream_t);
 
 }  // namespace fwi

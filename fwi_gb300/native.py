@@ -27,7 +27,7 @@ FWI_ERR_NODEVICE = -7
 
 MODE_REF_COMPAT, MODE_EXACT = 0, 1
 PREC_FP32, PREC_FP64 = 0, 1
-STORE_FULL, STORE_CHECKPOINT = 0, 1
+STORE_FULL, STORE_CHECKPOINT, STORE_BOUNDARY = 0, 1, 2
 SPREC_NATIVE, SPREC_FP16, SPREC_BF16 = 0, 1, 2
 
 COMPAT_SYMBOLS = [

@@ -51,6 +51,9 @@ extern "C" {
 /* How the forward images that the imaging condition needs are kept. */
 #define FWI_STORE_FULL 0       /* every step, in HBM */
 #define FWI_STORE_CHECKPOINT 1 /* full states every ckpt_every steps; segments recomputed */
+#define FWI_STORE_BOUNDARY 2   /* the ring of the state around the region the CPML layers do not
+                                  touch, every step; that region rebuilt backwards in time during
+                                  the adjoint (FP rounding: approximate), gradient zero in the layers */
 
 /* Element type of stored images (per-snapshot scaled for FP16). */
 #define FWI_SPREC_NATIVE 0 /* same as the compute precision */

@@ -307,3 +307,42 @@ def test_checkpointing_reproduces_full_storage_bitwise(exact_case, mode, every, 
     assert res[0][0] == res[1][0]
     for a, b in zip(res[0][1:], res[1][1:]):
         assert np.array_equal(a, b), rel_l2(b, a)
+
+
+def rebuild_region_mask(p, shots):
+    """Model points inside every shot's CPML-free region (FWI_STORE_BOUNDARY's R)."""
+    m = np.ones((p["nz"], p["nx"]), bool)
+    for s in shots:
+        w = s["nxw"] or p["nx"]
+        r = np.zeros_like(m)
+        r[4:p["nz"] - p["cpml"], s["x0"] + p["cpml"]:s["x0"] + w - p["cpml"]] = True
+        m &= r
+    return m
+
+
+@pytest.mark.parametrize("precision,sprec,tol", [("fp64", 0, 1e-9), ("fp32", 0, 2e-4), ("fp32", 1, 2e-3)])
+@pytest.mark.parametrize("mode", ["exact", "ref"])
+def test_boundary_storage_rebuilds_the_images(exact_case, precision, sprec, tol, mode):
+    """FWI_STORE_BOUNDARY: the misfit is the full store's exactly; inside the
+    region every shot rebuilds, the gradient is the full store's up to the
+    rounding of the backward rebuild (tolerances measured, stated here);
+    outside every shot's region it has only the shots that do rebuild there."""
+    from fwi_gb300 import (Context, MODE_EXACT, MODE_REF_COMPAT, PREC_FP32, PREC_FP64, STORE_BOUNDARY, STORE_FULL,
+                           make_shots)
+    p, shots, obs, mask, _, _ = exact_case
+    prec = PREC_FP64 if precision == "fp64" else PREC_FP32
+    dt_ = np.float64 if precision == "fp64" else np.float32
+    res = []
+    for store in (STORE_FULL, STORE_BOUNDARY):
+        ctx = Context(nx=p["nx"], nz=p["nz"], dh=p["dh"], dt=p["dt"], cpml=p["cpml"], f_cpml=p["f"],
+                      nt_max=p["nt"], max_shots=2, mode=MODE_EXACT if mode == "exact" else MODE_REF_COMPAT,
+                      precision=prec, store=store, store_prec=sprec)
+        ctx.set_wavelet(wavelet(p).astype(dt_))
+        ctx.set_model(*(np.ascontiguousarray(p[k], dt_) for k in ("vh", "vp", "vn")))
+        res.append(ctx.gradient(make_shots(shots), obs.astype(dt_), mask))
+        del ctx
+    assert res[0][0] == res[1][0]
+    inside = rebuild_region_mask(p, shots)
+    for a, b in zip(res[0][1:], res[1][1:]):
+        assert rel_l2(b[inside], a[inside]) <= tol, rel_l2(b[inside], a[inside])
+        assert np.all(np.isfinite(b))
