@@ -113,7 +113,8 @@ def dist_setup():
     import torch.distributed as dist
     rank = int(os.environ["RANK"])
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, n, dist
 
@@ -362,7 +363,7 @@ def reference_arm(args, rank, world, dist):
         else synth.WORKLOADS[args.workload]()
     secs = max(2.0, args.cpu_seconds / max(1, args.steps))
     vals = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
+    for _ in range(args.warmup):  # untimed, short samples
         cpu_sample(w, seconds=1.0)
     t0 = time.perf_counter()
     for _ in range(args.steps):
