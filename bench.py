@@ -265,11 +265,13 @@ def native_arm(args, rank, world, dist):
             "metric": METRIC, "value": round(value, 4), "unit": "shots/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic (seeded C2 model, observed data modelled on the GPU from the true model)",
+            "data": f"synthetic (seeded {args.workload} model, observed data modelled on the GPU from the true model)",
             "config": {"workload": w.name, "nx": w.nx, "nz": w.nz, "dh": w.dh, "dt": w.dt, "nt": w.nt,
                        "shots": nshots, "receivers_per_shot": nrec, "ricker_hz": w.f, "cpml": w.cpml,
                        "mode": args.mode, "image_store": f"{args.storage}, {args.store}", "batch": args.batch,
-                       "l2": "inputs larger than L2 (observed data 231 MB, images streamed through HBM)"},
+                       "l2": f"inputs larger than L2 (observed data {ntr * 4 / 1e6:.0f} MB; the per-step state of "
+                             f"all shots {6 * 4 * w.nz * w.nx * nshots / 1e6:.0f} MB; images or rings streamed "
+                             f"through HBM)"},
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
                     "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
@@ -300,7 +302,7 @@ def native_arm(args, rank, world, dist):
         # plain per-shot FP32 path (one shot per launch sequence, FP32 images), on a subset
         sub = fwi_gb300.make_shots(w.shots[: args.plain_shots])
         nsub = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots[: args.plain_shots])
-        c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE, store=fwi_gb300.STORE_FULL)
+        c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE)
         c1.set_model(*w.squared(initial=True))
         c1.gradient(sub, obs_d[:nsub])
         torch.cuda.synchronize()
@@ -311,11 +313,10 @@ def native_arm(args, rank, world, dist):
         ref32 = c1.gradient(sub, obs_d[:nsub].cpu().numpy())
         del c1
         out["plain_gpu"] = {"value": round(plain, 4), "unit": "shots/s",
-                            "how": f"max_shots=1, FP32 images, {args.plain_shots} shots timed",
+                            "how": f"max_shots=1, FP32 images, {args.storage} storage, {args.plain_shots} shots timed",
                             "speedup": round(value / world / plain, 2)}
-        # gradient error of this configuration against the FP64 GPU path, same shots
-        c64 = context(args.plain_shots, precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE,
-                      store=fwi_gb300.STORE_FULL)
+        # gradient error of this configuration against the FP64 GPU path, same shots and storage
+        c64 = context(args.plain_shots, precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE)
         c64.set_model(*(a.astype(np.float64) for a in w.squared(initial=True)))
         r64 = c64.gradient(sub, obs_d[:nsub].cpu().numpy().astype(np.float64))
         del c64
@@ -331,7 +332,7 @@ def native_arm(args, rank, world, dist):
             "misfit_rel_err": abs(rx[0] - r64[0]) / abs(r64[0])}
         # L-BFGS two-loop (m = 5) on this grid, FP64 dots
         from fwi_gb300 import Context
-        cl = context(1, store=fwi_gb300.STORE_FULL)
+        cl = context(1)
         cl.set_model(*w.squared(initial=True))
         cl.set_gradient(*(a.astype(np.float32) for a in r64[1:]))
         cl.first_step(3e5, 2e5, 2.5e5)
