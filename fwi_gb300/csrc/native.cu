@@ -655,6 +655,7 @@ template <typename T> struct Ctx : CtxBase {
             store = q0;
         }
         if (sizeof(T) == sizeof(float)) {
+            TRY(fwi::prepare_fp32_kernels());
             int rc = build_maps(maps, lvl, cp);
             if (rc == FWI_OK && cfg.store == FWI_STORE_CHECKPOINT) {
                 // the recompute's forward steps use its own first 4 CPML arrays

@@ -145,6 +145,10 @@ template <typename T>
 void launch_adjoint_step(const Batch<T> &b, int nx_max, int j, int ntb, int cur, int zsel,
                          bool exact, int img_base, const StepStreams &ss);
 
+// Sets the FP32 tile kernels' dynamic shared-memory limit on the current
+// device (once per device); call before their first launch there.
+cudaError_t prepare_fp32_kernels();
+
 // Boundary storage (prop_boundary.cuh): ring length per shot, saving the
 // ring of step g, and the backward rebuild of the CPML-free region.
 long boundary_ring_len(int nx_max, int nz, int cpml);

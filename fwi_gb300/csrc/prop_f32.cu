@@ -6,6 +6,8 @@
 //   main stream:  interior tiles (prop_tma.cuh)
 // joined before the next step.  Both tile passes read only the current time
 // level and write disjoint points.  The generic passes of prop.cuh serve FP64.
+#include <mutex>
+
 #include "prop_boundary.cuh"
 #include "prop_layer.cuh"
 
@@ -13,9 +15,9 @@ namespace fwi {
 
 namespace {
 
-template <typename K> void allow_smem(K kernel, size_t bytes)
+template <typename K> cudaError_t allow_smem(K kernel, size_t bytes)
 {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 // Tiles from the grid origin (b.xbase, b.zbase) to the window's far edges.
@@ -26,9 +28,7 @@ inline dim3 tma_grid(const Batch<float> &b, int nx_max, int sg)
 
 template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
 {
-    static bool set = false;
     const size_t sm = fwd_tma_smem();
-    if (!set) { allow_smem(k_fwd_tma<ST>, sm); set = true; }
     k_fwd_tma<ST><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, *static_cast<const TmaMaps *>(b.tma), g,
                                                                        ntb, cur, slot, b.sg);
 }
@@ -36,9 +36,7 @@ template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, in
 template <int ST, bool EXACT, bool INLINE>
 void fwd_layer(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
 {
-    static bool set = false;
     const size_t sm = fwd_layer_smem();
-    if (!set) { allow_smem(k_fwd_layer<ST, EXACT, INLINE>, sm); set = true; }
     k_fwd_layer<ST, EXACT, INLINE><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
         b, *static_cast<const TmaMaps *>(b.tma), g, ntb, cur, slot, b.sg_layer);
 }
@@ -46,9 +44,7 @@ void fwd_layer(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int s
 template <int ST, bool EXACT>
 void adj_interior(const Batch<float> &b, int nx_max, int j, int ntb, int cur, int zsel, int base, cudaStream_t st)
 {
-    static bool set = false;
     const size_t sm = adj_tma_smem();
-    if (!set) { allow_smem(k_adj_tma<ST, EXACT>, sm); set = true; }
     k_adj_tma<ST, EXACT><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(
         b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, base, b.sg);
 }
@@ -56,9 +52,7 @@ void adj_interior(const Batch<float> &b, int nx_max, int j, int ntb, int cur, in
 template <int ST, bool EXACT, bool INLINE>
 void adj_layer(const Batch<float> &b, int nx_max, int j, int ntb, int cur, int zsel, int base, cudaStream_t st)
 {
-    static bool set = false;
     const size_t sm = adj_layer_smem();
-    if (!set) { allow_smem(k_adj_layer<ST, EXACT, INLINE>, sm); set = true; }
     k_adj_layer<ST, EXACT, INLINE><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
         b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, base, b.sg_layer);
 }
@@ -128,7 +122,42 @@ void adjoint_step(const Batch<float> &b, int nx_max, int j, int ntb, int cur, in
         });
 }
 
+template <int ST> cudaError_t allow_all()
+{
+    cudaError_t e = cudaSuccess;
+    auto keep = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+    keep(allow_smem(k_fwd_tma<ST>, fwd_tma_smem()));
+    keep(allow_smem(k_fwd_layer<ST, true, true>, fwd_layer_smem()));
+    keep(allow_smem(k_fwd_layer<ST, true, false>, fwd_layer_smem()));
+    keep(allow_smem(k_fwd_layer<ST, false, true>, fwd_layer_smem()));
+    keep(allow_smem(k_fwd_layer<ST, false, false>, fwd_layer_smem()));
+    keep(allow_smem(k_adj_tma<ST, true>, adj_tma_smem()));
+    keep(allow_smem(k_adj_tma<ST, false>, adj_tma_smem()));
+    keep(allow_smem(k_adj_layer<ST, true, true>, adj_layer_smem()));
+    keep(allow_smem(k_adj_layer<ST, true, false>, adj_layer_smem()));
+    keep(allow_smem(k_adj_layer<ST, false, true>, adj_layer_smem()));
+    keep(allow_smem(k_adj_layer<ST, false, false>, adj_layer_smem()));
+    return e;
+}
+
 }  // namespace
+
+// Dynamic shared memory above 48 KB for every FP32 tile kernel: a function
+// attribute of the current device's context, set once per device.
+cudaError_t prepare_fp32_kernels()
+{
+    static std::mutex mu;
+    static bool done[256] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev >= 0 && dev < 256 && done[dev]) return cudaSuccess;
+    for (cudaError_t r : {allow_all<kStoreNative>(), allow_all<kStoreHalf>(), allow_all<kStoreBf16>()})
+        if (r != cudaSuccess) return r;
+    if (dev >= 0 && dev < 256) done[dev] = true;
+    return cudaSuccess;
+}
 
 template <>
 void launch_forward_step<float>(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int img_slot,
