@@ -541,9 +541,13 @@ template <typename T> struct Ctx : CtxBase {
     // batch
     T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {};
     void *store = nullptr;
-    // boundary storage: ring of every step [B][nt_max][ring_len], rebuild state in rlvl
+    // boundary storage: ring of every step [B][nt_max][ring_len], rebuild state in rlvl;
+    // the rebuild runs on its own stream one step ahead of the adjoint, images
+    // alternating between 2 slots (slot = step & 1)
     T *ring = nullptr;
     long ring_len = 0;
+    cudaStream_t rst = nullptr;
+    cudaEvent_t ev_rfork = nullptr, ev_reb[2] = {}, ev_adj[2] = {};
     // checkpointing: full states every ck_every steps, segment recompute buffers
     int ck_every = 0, n_ck = 0;
     T *ck = nullptr;                 // [n_ck][8][B * slot]: P, F, their increments, CPML x4
@@ -575,8 +579,15 @@ template <typename T> struct Ctx : CtxBase {
         if (st) cudaStreamSynchronize(st);
         for (void *p : allocs) cudaFree(p);
         if (ss.side) cudaStreamSynchronize(ss.side);
+        if (rst) cudaStreamSynchronize(rst);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
+        for (int k = 0; k < 2; k++) {
+            if (ev_reb[k]) cudaEventDestroy(ev_reb[k]);
+            if (ev_adj[k]) cudaEventDestroy(ev_adj[k]);
+        }
+        if (ev_rfork) cudaEventDestroy(ev_rfork);
+        if (rst) cudaStreamDestroy(rst);
         for (cudaEvent_t e : {ss.fork, ss.join})
             if (e) cudaEventDestroy(e);
         if (ss.side) cudaStreamDestroy(ss.side);
@@ -644,9 +655,15 @@ template <typename T> struct Ctx : CtxBase {
         }
         if (cfg.store == FWI_STORE_BOUNDARY) {
             ring_len = fwi::boundary_ring_len(win, nz, cfg.cpml);
-            n_img = 1;  // the image of the step just rebuilt
+            n_img = 2;  // the images of the last two steps rebuilt
             TRY(alloc(&ring, (size_t)B * nt_max * ring_len));
             for (auto &p : rlvl) TRY(alloc(&p, (size_t)B * slot));
+            TRY(cudaStreamCreateWithFlags(&rst, cudaStreamNonBlocking));
+            TRY(cudaEventCreateWithFlags(&ev_rfork, cudaEventDisableTiming));
+            for (int k = 0; k < 2; k++) {
+                TRY(cudaEventCreateWithFlags(&ev_reb[k], cudaEventDisableTiming));
+                TRY(cudaEventCreateWithFlags(&ev_adj[k], cudaEventDisableTiming));
+            }
         }
         {
             void *q0 = nullptr;
@@ -657,6 +674,7 @@ template <typename T> struct Ctx : CtxBase {
         if (sizeof(T) == sizeof(float)) {
             TRY(fwi::prepare_fp32_kernels());
             int rc = build_maps(maps, lvl, cp);
+            if (rc == FWI_OK && cfg.store == FWI_STORE_BOUNDARY) rc = build_maps(rmaps, rlvl, cp);  // rebuild levels
             if (rc == FWI_OK && cfg.store == FWI_STORE_CHECKPOINT) {
                 // the recompute's forward steps use its own first 4 CPML arrays
                 T *const rcpv[8] = {rcp[0], rcp[1], rcp[2], rcp[3], cp[4], cp[5], cp[6], cp[7]};
@@ -1059,23 +1077,37 @@ template <typename T> struct Ctx : CtxBase {
                     const int lag = exact ? 0 : 1;
                     Batch<T> rb = b;
                     for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
-                    fwi::launch_rebuild_begin<T>(rb, nxm, ntb - 1, ntb, 0, ring, ring_len, st);
+                    rb.tma = use_tma ? (const void *)&rmaps : nullptr;
+                    // the rebuild stream starts after everything issued so far (the final state copies)
+                    TRY(cudaEventRecord(ev_rfork, st));
+                    TRY(cudaStreamWaitEvent(rst, ev_rfork, 0));
+                    fwi::launch_rebuild_begin<T>(rb, nxm, ntb - 1, ntb, 0, ring, ring_len, rst);
                     launches += 2;
                     int rcur = 1, next_g = ntb - 1;
                     for (int j = 0; j < ntb; j++) {
                         const int need = ntb - 1 - lag - j;
                         for (; next_g >= 0 && next_g >= need; next_g--) {
-                            fwi::launch_rebuild_step<T>(rb, nxm, next_g, ntb, rcur, ring, ring_len, st);
+                            // slot next_g & 1 is free once the adjoint iteration imaging step next_g + 2 is done
+                            TRY(cudaStreamWaitEvent(rst, ev_adj[next_g & 1], 0));
+                            fwi::launch_rebuild_step<T>(rb, nxm, next_g, ntb, rcur, ring, ring_len, next_g & 1, rst);
+                            TRY(cudaEventRecord(ev_reb[next_g & 1], rst));
                             rcur ^= 1;
-                            launches += 2;
+                            launches += sizeof(T) == 4 ? 1 : 2;
                         }
+                        if (need >= 0) TRY(cudaStreamWaitEvent(st, ev_reb[need & 1], 0));
                         fwi::StepStreams sst = ss;
                         sample(1, j, sst);
-                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, need >= 0 ? need : 0, sst);
+                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, need >= 0 ? need - (need & 1) : 0,
+                                                    sst);
+                        if (need >= 0) TRY(cudaEventRecord(ev_adj[need & 1], st));
                         cur ^= 1;
                         zsel ^= 1;
                         launches += kps;
                     }
+                    // the main stream is past every rebuild: the last adjoint iteration with an
+                    // image waited for it; join the rebuild stream all the same
+                    TRY(cudaEventRecord(ev_reb[0], rst));
+                    TRY(cudaStreamWaitEvent(st, ev_reb[0], 0));
                     TRY_LAUNCH();
                 } else if (!ckpt) {
                     for (int j = 0; j < ntb; j++) {
@@ -1402,7 +1434,7 @@ size_t fwi_config_bytes(const fwi_config *c)
         b += (size_t)c->max_shots * k * 2 * slot * se;       // images of one segment
     } else if (c->store == FWI_STORE_BOUNDARY) {
         b += (size_t)c->max_shots * c->nt_max * fwi::boundary_ring_len((int)win, c->nz, c->cpml) * e;  // rings
-        b += (size_t)c->max_shots * slot * (6 * e + 2 * se);  // rebuild state, one image
+        b += (size_t)c->max_shots * slot * (6 * e + 4 * se);  // rebuild state, two images
     } else {
         b += (size_t)c->max_shots * c->nt_max * 2 * slot * se; // images
     }

@@ -42,10 +42,13 @@ __device__ __forceinline__ T coef_z(const T *tab, int iz, int nz, int cpml)
 // ---------------------------------------------------------------- image store codecs
 
 template <typename T, int ST> struct Codec;
+// enc(v, sc, status) reports saturation at once; enc_flag(v, sc, sat) only
+// sets `sat` (NaN included), for callers that report once per thread.
 template <typename T> struct Codec<T, kStoreNative> {
     using S = T;
     static constexpr bool scaled = false;
     static __device__ __forceinline__ S enc(T v, float, unsigned *) { return v; }
+    static __device__ __forceinline__ S enc_flag(T v, float, bool &) { return v; }
     static __device__ __forceinline__ T dec(S v, float) { return v; }  // second argument: inverse scale
 };
 template <typename T> struct Codec<T, kStoreHalf> {
@@ -60,12 +63,19 @@ template <typename T> struct Codec<T, kStoreHalf> {
         }
         return __float2half_rn(x);
     }
+    static __device__ __forceinline__ S enc_flag(T v, float sc, bool &sat)
+    {
+        const float x = (float)v * sc;
+        sat |= !(fabsf(x) <= 65504.f);
+        return __float2half_rn(fminf(fmaxf(x, -65504.f), 65504.f));
+    }
     static __device__ __forceinline__ T dec(S v, float inv_sc) { return (T)(__half2float(v) * inv_sc); }
 };
 template <typename T> struct Codec<T, kStoreBf16> {
     using S = __nv_bfloat16;
     static constexpr bool scaled = true;
     static __device__ __forceinline__ S enc(T v, float sc, unsigned *) { return __float2bfloat16_rn((float)v * sc); }
+    static __device__ __forceinline__ S enc_flag(T v, float sc, bool &) { return __float2bfloat16_rn((float)v * sc); }
     static __device__ __forceinline__ T dec(S v, float inv_sc) { return (T)(__bfloat162float(v) * inv_sc); }
 };
 

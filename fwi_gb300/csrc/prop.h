@@ -160,6 +160,6 @@ void launch_rebuild_begin(const Batch<T> &rb, int nx_max, int g, int ntb, int sr
                           cudaStream_t st);
 template <typename T>
 void launch_rebuild_step(const Batch<T> &rb, int nx_max, int g, int ntb, int cur, const T *ring, long ring_len,
-                         cudaStream_t st);
+                         int img_slot, cudaStream_t st);
 
 }  // namespace fwi

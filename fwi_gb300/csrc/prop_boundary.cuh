@@ -177,13 +177,13 @@ template <typename T> void launch_rebuild_begin(const Batch<T> &rb, int nx_max, 
 }
 
 template <typename T> void launch_rebuild_step(const Batch<T> &rb, int nx_max, int g, int ntb, int cur,
-                                               const T *ring, long ring_len, cudaStream_t st)
+                                               const T *ring, long ring_len, int img_slot, cudaStream_t st)
 {
     const dim3 blk(32, 8), grid((nx_max + 31) / 32, (rb.nz + 7) / 8, rb.B);
     switch (rb.store_type) {
-    case kStoreHalf: k_rebuild_step<T, kStoreHalf><<<grid, blk, 0, st>>>(rb, g, ntb, cur, 0); break;
-    case kStoreBf16: k_rebuild_step<T, kStoreBf16><<<grid, blk, 0, st>>>(rb, g, ntb, cur, 0); break;
-    default: k_rebuild_step<T, kStoreNative><<<grid, blk, 0, st>>>(rb, g, ntb, cur, 0); break;
+    case kStoreHalf: k_rebuild_step<T, kStoreHalf><<<grid, blk, 0, st>>>(rb, g, ntb, cur, img_slot); break;
+    case kStoreBf16: k_rebuild_step<T, kStoreBf16><<<grid, blk, 0, st>>>(rb, g, ntb, cur, img_slot); break;
+    default: k_rebuild_step<T, kStoreNative><<<grid, blk, 0, st>>>(rb, g, ntb, cur, img_slot); break;
     }
     const long n = Ring::make(nx_max, rb.nz, rb.cpml).count();
     k_load_ring<T><<<dim3((unsigned)std::max(1L, (n + 255) / 256), rb.B), 256, 0, st>>>(rb, g - 1, ntb, 1 - cur, ring,

@@ -10,6 +10,7 @@
 
 #include "prop_boundary.cuh"
 #include "prop_layer.cuh"
+#include "prop_rebuild.cuh"
 
 namespace fwi {
 
@@ -137,6 +138,7 @@ template <int ST> cudaError_t allow_all()
     keep(allow_smem(k_adj_layer<ST, true, false>, adj_layer_smem()));
     keep(allow_smem(k_adj_layer<ST, false, true>, adj_layer_smem()));
     keep(allow_smem(k_adj_layer<ST, false, false>, adj_layer_smem()));
+    keep(allow_smem(k_rebuild_tma<ST>, rebuild_tma_smem()));
     return e;
 }
 
@@ -186,7 +188,19 @@ long boundary_ring_len(int nx_max, int nz, int cpml) { return Ring::make(nx_max,
 template void launch_save_ring<float>(const Batch<float> &, int, int, int, int, float *, long, cudaStream_t);
 template void launch_rebuild_begin<float>(const Batch<float> &, int, int, int, int, const float *, long,
                                           cudaStream_t);
-template void launch_rebuild_step<float>(const Batch<float> &, int, int, int, int, const float *, long,
-                                         cudaStream_t);
+// The tiled rebuild (prop_rebuild.cuh): one launch per step, the next level's ring included.
+template <>
+void launch_rebuild_step<float>(const Batch<float> &rb, int nx_max, int g, int ntb, int cur, const float *ring,
+                                long ring_len, int img_slot, cudaStream_t st)
+{
+    const dim3 grid = tma_grid(rb, nx_max, rb.sg);
+    const size_t sm = rebuild_tma_smem();
+    const TmaMaps &m = *static_cast<const TmaMaps *>(rb.tma);
+    switch (rb.store_type) {
+    case kStoreHalf: k_rebuild_tma<kStoreHalf><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, rb.sg, img_slot); break;
+    case kStoreBf16: k_rebuild_tma<kStoreBf16><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, rb.sg, img_slot); break;
+    default: k_rebuild_tma<kStoreNative><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, rb.sg, img_slot); break;
+    }
+}
 
 }  // namespace fwi

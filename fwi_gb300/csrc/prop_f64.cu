@@ -9,6 +9,6 @@ template void launch_adjoint_step<double>(const Batch<double> &, int, int, int, 
 template void launch_save_ring<double>(const Batch<double> &, int, int, int, int, double *, long, cudaStream_t);
 template void launch_rebuild_begin<double>(const Batch<double> &, int, int, int, int, const double *, long,
                                            cudaStream_t);
-template void launch_rebuild_step<double>(const Batch<double> &, int, int, int, int, const double *, long,
+template void launch_rebuild_step<double>(const Batch<double> &, int, int, int, int, const double *, long, int,
                                           cudaStream_t);
 }  // namespace fwi

@@ -277,10 +277,12 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
                 SI *img = (SI *)b.store + sh.img;
                 SI eG[4], eH[4];
 #pragma unroll
+                bool sat = false;
                 for (int q = 0; q < 4; q++) {
-                    eG[q] = Cd::enc(m[q] ? (EXACT ? G[q] : gP[q]) : 0.f, sh.sc, b.status);
-                    eH[q] = Cd::enc(m[q] ? (EXACT ? H[q] : gF[q]) : 0.f, sh.sc, b.status);
+                    eG[q] = Cd::enc_flag(m[q] ? (EXACT ? G[q] : gP[q]) : 0.f, sh.sc, sat);
+                    eH[q] = Cd::enc_flag(m[q] ? (EXACT ? H[q] : gF[q]) : 0.f, sh.sc, sat);
                 }
+                if (sat) atomicOr(b.status, kStatusSaturated);
                 if (all) {
                     Vec4Store<SI>::put(img + ipt, eG);
                     Vec4Store<SI>::put(img + b.slot + ipt, eH);

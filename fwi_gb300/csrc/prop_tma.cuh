@@ -321,10 +321,12 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
                 const float sc = sh.sc;
                 SI eG[4], eH[4];
 #pragma unroll
+                bool sat = false;
                 for (int q = 0; q < 4; q++) {
-                    eG[q] = Cd::enc(m[q] ? gG[q] : 0.f, sc, b.status);
-                    eH[q] = Cd::enc(m[q] ? gH[q] : 0.f, sc, b.status);
+                    eG[q] = Cd::enc_flag(m[q] ? gG[q] : 0.f, sc, sat);
+                    eH[q] = Cd::enc_flag(m[q] ? gH[q] : 0.f, sc, sat);
                 }
+                if (sat) atomicOr(b.status, kStatusSaturated);
                 if (all) {
                     Vec4Store<SI>::put(img + ipt, eG);
                     Vec4Store<SI>::put(img + b.slot + ipt, eH);
