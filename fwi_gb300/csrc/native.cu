@@ -424,13 +424,14 @@ __global__ void k_grad_vti(const T *vh, const T *vp, const T *vn, const T *gh, c
     }
 }
 
-// Steps between checkpoints: minimises checkpoint (8 full arrays each) plus
-// segment image memory (2 arrays of the image type per step) for nt steps.
+// Steps between checkpoints: minimises checkpoint memory (8 full arrays each,
+// nt / K of them) plus segment image memory (two segments in flight, 2
+// arrays of the image type per step: 4 K) for nt steps.
 int checkpoint_interval(const fwi_config &c)
 {
     if (c.ckpt_every > 0) return std::min(c.ckpt_every, c.nt_max);
     const double img = c.store_prec == FWI_SPREC_NATIVE ? 1.0 : 0.5 * (c.precision == FWI_PREC_FP64 ? 0.5 : 1.0);
-    int k = (int)std::ceil(std::sqrt(8.0 * c.nt_max / (2.0 * img)));
+    int k = (int)std::ceil(std::sqrt(8.0 * c.nt_max / (4.0 * img)));
     return std::max(1, std::min(k, c.nt_max));
 }
 
@@ -541,12 +542,14 @@ template <typename T> struct Ctx : CtxBase {
     // batch
     T *lvl[6] = {}, *cp[8] = {}, *gs[3] = {};
     void *store = nullptr;
-    // boundary storage: ring of every step [B][nt_max][ring_len], rebuild state in rlvl;
-    // the rebuild runs on its own stream one step ahead of the adjoint, images
-    // alternating between 2 slots (slot = step & 1)
+    // boundary storage: ring of every step [B][nt_max][ring_len], rebuild state in rlvl.
     T *ring = nullptr;
     long ring_len = 0;
+    // Checkpoint and boundary storage rebuild images on their own streams (rss)
+    // ahead of the adjoint, into two halves of the image buffer: ev_reb[h] =
+    // half h rebuilt, ev_adj[h] = half h consumed by the adjoint.
     cudaStream_t rst = nullptr;
+    fwi::StepStreams rss{};
     cudaEvent_t ev_rfork = nullptr, ev_reb[2] = {}, ev_adj[2] = {};
     // checkpointing: full states every ck_every steps, segment recompute buffers
     int ck_every = 0, n_ck = 0;
@@ -587,6 +590,10 @@ template <typename T> struct Ctx : CtxBase {
             if (ev_adj[k]) cudaEventDestroy(ev_adj[k]);
         }
         if (ev_rfork) cudaEventDestroy(ev_rfork);
+        if (rss.side) cudaStreamSynchronize(rss.side);
+        for (cudaEvent_t e : {rss.fork, rss.join})
+            if (e) cudaEventDestroy(e);
+        if (rss.side) cudaStreamDestroy(rss.side);
         if (rst) cudaStreamDestroy(rst);
         for (cudaEvent_t e : {ss.fork, ss.join})
             if (e) cudaEventDestroy(e);
@@ -648,7 +655,7 @@ template <typename T> struct Ctx : CtxBase {
         if (cfg.store == FWI_STORE_CHECKPOINT) {
             ck_every = checkpoint_interval(cfg);
             n_ck = (nt_max + ck_every - 1) / ck_every;
-            n_img = ck_every;
+            n_img = 2 * ck_every;  // two segments' images: one rebuilt while the other is consumed
             TRY(alloc(&ck, (size_t)n_ck * 8 * B * slot));
             for (auto &p : rlvl) TRY(alloc(&p, (size_t)B * slot));
             for (auto &p : rcp) TRY(alloc(&p, (size_t)B * slot));
@@ -658,11 +665,21 @@ template <typename T> struct Ctx : CtxBase {
             n_img = 2;  // the images of the last two steps rebuilt
             TRY(alloc(&ring, (size_t)B * nt_max * ring_len));
             for (auto &p : rlvl) TRY(alloc(&p, (size_t)B * slot));
+        }
+        if (cfg.store != FWI_STORE_FULL) {
             TRY(cudaStreamCreateWithFlags(&rst, cudaStreamNonBlocking));
             TRY(cudaEventCreateWithFlags(&ev_rfork, cudaEventDisableTiming));
             for (int k = 0; k < 2; k++) {
                 TRY(cudaEventCreateWithFlags(&ev_reb[k], cudaEventDisableTiming));
                 TRY(cudaEventCreateWithFlags(&ev_adj[k], cudaEventDisableTiming));
+            }
+            rss.main = rst;
+            if (ss.side) {  // the recompute's forward steps fork like the main ones
+                int lo = 0, hi = 0;
+                TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+                TRY(cudaStreamCreateWithPriority(&rss.side, cudaStreamNonBlocking, hi));
+                TRY(cudaEventCreateWithFlags(&rss.fork, cudaEventDisableTiming));
+                TRY(cudaEventCreateWithFlags(&rss.join, cudaEventDisableTiming));
             }
         }
         {
@@ -934,16 +951,16 @@ template <typename T> struct Ctx : CtxBase {
         return FWI_OK;
     }
 
-    int restore_checkpoint(int k, int nb, int cur)
+    int restore_checkpoint(int k, int nb, int cur, cudaStream_t s)
     {
         const size_t bytes = (size_t)nb * slot * sizeof(T);
         T *dst[8] = {rlvl[cur], rlvl[2 + cur], rlvl[4], rlvl[5], rcp[0], rcp[1], rcp[2], rcp[3]};
         for (int a = 0; a < 8; a++)
-            TRY(cudaMemcpyAsync(dst[a], ck + ((size_t)k * 8 + a) * B * slot, bytes, cudaMemcpyDeviceToDevice, st));
+            TRY(cudaMemcpyAsync(dst[a], ck + ((size_t)k * 8 + a) * B * slot, bytes, cudaMemcpyDeviceToDevice, s));
         // a shot that starts later inside the segment reads the other level when it starts:
         // give both levels the checkpointed state (zero for such a shot)
-        TRY(cudaMemcpyAsync(rlvl[1 - cur], ck + ((size_t)k * 8 + 0) * B * slot, bytes, cudaMemcpyDeviceToDevice, st));
-        TRY(cudaMemcpyAsync(rlvl[3 - cur], ck + ((size_t)k * 8 + 1) * B * slot, bytes, cudaMemcpyDeviceToDevice, st));
+        TRY(cudaMemcpyAsync(rlvl[1 - cur], ck + ((size_t)k * 8 + 0) * B * slot, bytes, cudaMemcpyDeviceToDevice, s));
+        TRY(cudaMemcpyAsync(rlvl[3 - cur], ck + ((size_t)k * 8 + 1) * B * slot, bytes, cudaMemcpyDeviceToDevice, s));
         return FWI_OK;
     }
 
@@ -1131,26 +1148,45 @@ template <typename T> struct Ctx : CtxBase {
                     rb.tma = use_tma ? (const void *)&rmaps : nullptr;
                     // `rec` holds the residuals now; the recomputed traces go to the spent obs copy
                     rb.rec = obs;
-                    int j = 0;
-                    for (int seg = (ntb - 1) / ck_every; seg >= 0; seg--) {
-                        const int a = seg * ck_every, e = std::min(a + ck_every, ntb);
+                    // segment seg's images go to half seg & 1 of the image buffer; the
+                    // recompute of segment seg - 1 (on rss) overlaps the adjoint iterations
+                    // imaging inside segment seg (on ss)
+                    TRY(cudaEventRecord(ev_rfork, st));
+                    TRY(cudaStreamWaitEvent(rst, ev_rfork, 0));
+                    auto recompute = [&](int seg) -> int {
+                        const int a = seg * ck_every, e = std::min(a + ck_every, ntb), h = seg & 1;
+                        TRY(cudaStreamWaitEvent(rst, ev_adj[h], 0));  // half h consumed (segment seg + 2)
                         int rcur = a & 1;
-                        int rc2 = restore_checkpoint(seg, nb, rcur);
+                        int rc2 = restore_checkpoint(seg, nb, rcur, rst);
                         if (rc2) return rc2;
                         for (int g = a; g < e; g++) {
-                            fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, g - a, exact, ss);
+                            fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, (g - a) + h * ck_every, exact, rss);
                             rcur ^= 1;
                         }
+                        TRY(cudaEventRecord(ev_reb[h], rst));
                         launches += kps * (e - a);
+                        return FWI_OK;
+                    };
+                    const int last = (ntb - 1) / ck_every;
+                    int rc3 = recompute(last);
+                    if (rc3) return rc3;
+                    int j = 0;
+                    for (int seg = last; seg >= 0; seg--) {
+                        const int a = seg * ck_every, h = seg & 1;
+                        if (seg > 0 && (rc3 = recompute(seg - 1))) return rc3;
+                        TRY(cudaStreamWaitEvent(st, ev_reb[h], 0));
                         for (; j < ntb && ntb - 1 - lag - j >= a; j++) {
                             fwi::StepStreams sst = ss;
                             sample(1, j, sst);
-                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a, sst);
+                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a - h * ck_every, sst);
                             cur ^= 1;
                             zsel ^= 1;
                             launches += kps;
                         }
+                        TRY(cudaEventRecord(ev_adj[h], st));
                     }
+                    TRY(cudaEventRecord(ev_reb[0], rst));  // join the recompute stream
+                    TRY(cudaStreamWaitEvent(st, ev_reb[0], 0));
                     for (; j < ntb; j++) {  // iterations without an image (reference lag)
                         fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, ss);
                         cur ^= 1;
@@ -1431,7 +1467,7 @@ size_t fwi_config_bytes(const fwi_config *c)
     if (c->store == FWI_STORE_CHECKPOINT) {
         const long k = checkpoint_interval(*c), n = (c->nt_max + k - 1) / k;
         b += (size_t)c->max_shots * slot * e * (8 * n + 10); // checkpoints, recompute state
-        b += (size_t)c->max_shots * k * 2 * slot * se;       // images of one segment
+        b += (size_t)c->max_shots * 2 * k * 2 * slot * se;   // images of two segments
     } else if (c->store == FWI_STORE_BOUNDARY) {
         b += (size_t)c->max_shots * c->nt_max * fwi::boundary_ring_len((int)win, c->nz, c->cpml) * e;  // rings
         b += (size_t)c->max_shots * slot * (6 * e + 4 * se);  // rebuild state, two images
