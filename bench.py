@@ -182,10 +182,13 @@ def native_arm(args, rank, world, dist):
     storage = {"full": fwi_gb300.STORE_FULL, "checkpoint": fwi_gb300.STORE_CHECKPOINT,
                "boundary": fwi_gb300.STORE_BOUNDARY}[args.storage]
 
+    # widest shot aperture (per-shot windows): per-shot arrays are sized by it, not by the model
+    max_window = max((s["nxw"] or w.nx) for s in w.shots)
+
     def context(max_shots, precision=fwi_gb300.PREC_FP32, store_prec=sprec, store=storage):
         c = fwi_gb300.Context(nx=w.nx, nz=w.nz, dh=w.dh, dt=w.dt, cpml=w.cpml, f_cpml=w.f, nt_max=w.nt,
-                              max_shots=max_shots, max_receivers=nrec, mode=mode, precision=precision,
-                              store_prec=store_prec, store=store, device=dev)
+                              max_shots=max_shots, max_receivers=nrec, max_window=max_window, mode=mode,
+                              precision=precision, store_prec=store_prec, store=store, device=dev)
         c.set_ricker(w.f, w.nt)
         return c
 

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -457,6 +458,16 @@ struct CtxBase {
     cudaEvent_t tev[2][kTimeSamples][2] = {};
     double tile_ms[2] = {0, 0}, tile_pts[2] = {0, 0};
     long tile_n[2] = {0, 0};
+    // CUDA graphs of the batch sections (Ctx<T>::run_section): on/off, replays so far
+    bool graphs = true;
+    long graph_replays = 0;
+    virtual void drop_sections() {}
+    int set_graphs(bool on)
+    {
+        if (!on) drop_sections();
+        graphs = on;
+        return FWI_OK;
+    }
 
     int set_tile_timing(bool on)
     {
@@ -558,6 +569,115 @@ template <typename T> struct Ctx : CtxBase {
     // TMA tensor maps of the batch buffers and of the recompute buffers (FP32 contexts)
     fwi::HostTmaMaps maps{}, rmaps{};
     bool use_tma = false;
+
+    // CUDA graphs of the two sections of a batch (the forward steps; the
+    // adjoint with its rebuild or recompute streams and the gradient sum).
+    // A section is keyed by every launch parameter it bakes in; it is issued
+    // directly the first time its key is seen, captured and instantiated the
+    // second time, replayed after that.  Every buffer it uses lives as long
+    // as the context, so a graph stays valid for its key.  FWI_GRAPHS=0:
+    // always direct.
+    struct Section {
+        std::vector<long> key;
+        cudaGraphExec_t exec = nullptr;
+        long launches = 0;              // kernel launches of the section
+        int phase = 0, nsamp = 0;       // tile timing samples it takes (phase, count, points)
+        double spts[kTimeSamples] = {};
+        unsigned long long used = 0;
+    };
+    static constexpr int kSections = 6;
+    std::vector<Section> sections;
+    unsigned long long section_clock = 0;
+
+    static void key_add(std::vector<long> &k, const void *p) { k.push_back((long)(uintptr_t)p); }
+    static void key_add(std::vector<long> &k, long v) { k.push_back(v); }
+    static void key_add(std::vector<long> &k, double v)
+    {
+        long bits = 0;
+        std::memcpy(&bits, &v, sizeof(bits));
+        k.push_back(bits);
+    }
+
+    // Every field of a batch view (the kernels take it by value).
+    static void key_batch(std::vector<long> &k, const Batch<T> &b)
+    {
+        for (long v : {(long)b.B, (long)b.nz, (long)b.pitch, (long)b.mpitch, (long)b.cpml, (long)b.nt_max, b.slot,
+                       (long)b.store_type, (long)b.n_img, (long)b.sg, (long)b.sg_layer, (long)b.xbase, (long)b.zbase,
+                       (long)b.inline_strip})
+            key_add(k, v);
+        for (const void *p : {(const void *)b.store, (const void *)b.scale, (const void *)b.amax,
+                              (const void *)b.rec, (const void *)b.shots, (const void *)b.mh, (const void *)b.mp,
+                              (const void *)b.mn, (const void *)b.cpa, (const void *)b.cpb, (const void *)b.wavelet,
+                              (const void *)b.status, b.tma})
+            key_add(k, p);
+        for (const T *p : b.lvl) key_add(k, (const void *)p);
+        for (const T *p : b.cp) key_add(k, (const void *)p);
+        for (const T *p : b.g) key_add(k, (const void *)p);
+        for (double v : {(double)b.inv_dh, (double)b.inv_dh2, (double)b.img_scale}) key_add(k, v);
+    }
+
+    void drop_sections() override
+    {
+        for (Section &s : sections)
+            if (s.exec) cudaGraphExecDestroy(s.exec);
+        sections.clear();
+    }
+
+    // Issues `body` (launches on st and on streams it joins back into st) as
+    // the section `key`: directly, or captured into a graph, or by replaying
+    // the graph.  The section's host bookkeeping (launch count, timing
+    // samples of `phase`: nsamp[phase] and the points row `spts`) is kept
+    // with it for the replays.
+    template <typename F> int run_section(const std::vector<long> &key, int phase, int *nsamp, double *spts, F body)
+    {
+        Section *s = nullptr;
+        for (Section &c : sections)
+            if (c.key == key) s = &c;
+        if (s && s->exec) {
+            s->used = ++section_clock;
+            TRY(cudaGraphLaunch(s->exec, st));
+            launches += s->launches;
+            nsamp[phase] = s->nsamp;
+            std::copy(s->spts, s->spts + kTimeSamples, spts);
+            graph_replays++;
+            return FWI_OK;
+        }
+        const bool capture = graphs && s != nullptr;
+        if (!s) {
+            if ((int)sections.size() >= kSections) {  // evict the least recently used
+                auto lru = std::min_element(sections.begin(), sections.end(),
+                                            [](const Section &a, const Section &c) { return a.used < c.used; });
+                if (lru->exec) cudaGraphExecDestroy(lru->exec);
+                sections.erase(lru);
+            }
+            sections.emplace_back();
+            s = &sections.back();
+            s->key = key;
+        }
+        s->used = ++section_clock;
+        s->phase = phase;
+        const long l0 = launches;
+        if (capture) TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = body();
+        if (capture) {
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc == FWI_OK && e == cudaSuccess)
+                e = cudaGraphInstantiateWithFlags(&s->exec, g, cudaGraphInstantiateFlagUseNodePriority);
+            if (g) cudaGraphDestroy(g);
+            if (rc != FWI_OK) return rc;
+            if (e != cudaSuccess) {
+                s->exec = nullptr;
+                return fail(e);
+            }
+            TRY(cudaGraphLaunch(s->exec, st));  // the captured work has not run yet
+        }
+        if (rc != FWI_OK) return rc;
+        s->launches = launches - l0;
+        s->nsamp = nsamp[phase];
+        std::copy(spts, spts + kTimeSamples, s->spts);
+        return FWI_OK;
+    }
     float *scale = nullptr, *amax = nullptr;
     T *rec = nullptr, *obs = nullptr;
     unsigned char *mask = nullptr;
@@ -580,6 +700,7 @@ template <typename T> struct Ctx : CtxBase {
     ~Ctx() override
     {
         if (st) cudaStreamSynchronize(st);
+        drop_sections();
         for (void *p : allocs) cudaFree(p);
         if (ss.side) cudaStreamSynchronize(ss.side);
         if (rst) cudaStreamSynchronize(rst);
@@ -632,6 +753,7 @@ template <typename T> struct Ctx : CtxBase {
         mslot = (long)nz * mpitch;
         n_img = nt_max;
         TRY(cudaSetDevice(cfg.device));
+        if (const char *e = getenv("FWI_GRAPHS")) graphs = atoi(e) != 0;
         TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         for (auto &e : ev) TRY(cudaEventCreate(&e));
         ss.main = st;
@@ -1035,7 +1157,7 @@ template <typename T> struct Ctx : CtxBase {
             const bool timed = tile_timing && sizeof(T) == 4;
             const int tstride = std::max(1, ntb / kTimeSamples);
             int nsamp[2] = {0, 0};
-            double spts[2][kTimeSamples];
+            double spts[2][kTimeSamples] = {};
             auto sample = [&](int phase, int step, fwi::StepStreams &sst) {
                 if (!timed || step % tstride != tstride / 2 || nsamp[phase] >= kTimeSamples) return;
                 const int aw = phase == 0 || !exact ? cfg.cpml : cfg.cpml + fwi::kRad;
@@ -1048,30 +1170,48 @@ template <typename T> struct Ctx : CtxBase {
                 sst.t0 = tev[phase][k][0];
                 sst.t1 = tev[phase][k][1];
             };
-            int cur = 0;
-            for (int g = 0; g < ntb; g++) {
-                if (ckpt && g % ck_every == 0) {
-                    int rc2 = save_checkpoint(g / ck_every, nb, cur);
-                    if (rc2) return rc2;
+            // launch parameters the sections bake in besides the batch view: the
+            // section, the step counts and storage, and each shot's steps and width
+            // (which shots run at a step, the timing samples' points)
+            auto section_key = [&](long tag) {
+                std::vector<long> k = {tag, nb, ntb, nxm, exact, want_grad, ckpt, bnd, ck_every, timed, tstride,
+                                       nslots};
+                key_batch(k, b);
+                for (const DevShot &d : bs) {
+                    k.push_back(d.nt);
+                    k.push_back(d.nx);
                 }
-                fwi::StepStreams sst = ss;
-                sample(0, g, sst);
-                if (bnd) fwi::launch_save_ring<T>(b, nxm, g, ntb, cur, ring, ring_len, st);
-                fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt && !bnd) ? g : -1, exact, sst);
-                cur ^= 1;
-            }
-            TRY_LAUNCH();
-            launches += (kps + (bnd ? 1 : 0)) * ntb;
-            if (bnd) {
-                // the final state (P, F, increments) starts the backward rebuild
-                for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
-                TRY(cudaMemcpyAsync(rlvl[0], lvl[cur], lb, cudaMemcpyDeviceToDevice, st));
-                TRY(cudaMemcpyAsync(rlvl[2], lvl[2 + cur], lb, cudaMemcpyDeviceToDevice, st));
-                TRY(cudaMemcpyAsync(rlvl[4], lvl[4], lb, cudaMemcpyDeviceToDevice, st));
-                TRY(cudaMemcpyAsync(rlvl[5], lvl[5], lb, cudaMemcpyDeviceToDevice, st));
-                // images of the layer points stay zero
-                TRY(cudaMemsetAsync(store, 0, (size_t)nb * n_img * 2 * slot * store_elem(), st));
-            }
+                return k;
+            };
+            rc = run_section(section_key(0), 0, nsamp, spts[0], [&]() -> int {
+                int cur = 0;
+                for (int g = 0; g < ntb; g++) {
+                    if (ckpt && g % ck_every == 0) {
+                        int rc2 = save_checkpoint(g / ck_every, nb, cur);
+                        if (rc2) return rc2;
+                    }
+                    fwi::StepStreams sst = ss;
+                    sample(0, g, sst);
+                    if (bnd) fwi::launch_save_ring<T>(b, nxm, g, ntb, cur, ring, ring_len, st);
+                    fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt && !bnd) ? g : -1, exact,
+                                                sst);
+                    cur ^= 1;
+                }
+                TRY_LAUNCH();
+                launches += (kps + (bnd ? 1 : 0)) * ntb;
+                if (bnd) {
+                    // the final state (P, F, increments) starts the backward rebuild
+                    for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+                    TRY(cudaMemcpyAsync(rlvl[0], lvl[cur], lb, cudaMemcpyDeviceToDevice, st));
+                    TRY(cudaMemcpyAsync(rlvl[2], lvl[2 + cur], lb, cudaMemcpyDeviceToDevice, st));
+                    TRY(cudaMemcpyAsync(rlvl[4], lvl[4], lb, cudaMemcpyDeviceToDevice, st));
+                    TRY(cudaMemcpyAsync(rlvl[5], lvl[5], lb, cudaMemcpyDeviceToDevice, st));
+                    // images of the layer points stay zero
+                    TRY(cudaMemsetAsync(store, 0, (size_t)nb * n_img * 2 * slot * store_elem(), st));
+                }
+                return FWI_OK;
+            });
+            if (rc) return rc;
             TRY(cudaEventRecord(e1, st));
             if (obs_in) {
                 k_residual<T><<<dim3(kRedBlocks, nb), kRedThreads, 0, st>>>(rec, obs, mask_in ? mask : nullptr, shots,
@@ -1083,122 +1223,133 @@ template <typename T> struct Ctx : CtxBase {
             if (traces)
                 TRY(cudaMemcpyAsync((T *)traces + off[b0], rec, nrec_elems * sizeof(T), cudaMemcpyDefault, st));
             if (want_grad) {
-                for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
-                for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
-                for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
-                cur = 0;
-                int zsel = 0;
-                if (bnd) {
-                    // rebuild the CPML-free region backwards one step ahead of the adjoint
-                    // iteration that images it (image slot 0 holds the step just rebuilt)
-                    const int lag = exact ? 0 : 1;
-                    Batch<T> rb = b;
-                    for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
-                    rb.tma = use_tma ? (const void *)&rmaps : nullptr;
-                    // the rebuild stream starts after everything issued so far (the final state copies)
-                    TRY(cudaEventRecord(ev_rfork, st));
-                    TRY(cudaStreamWaitEvent(rst, ev_rfork, 0));
-                    fwi::launch_rebuild_begin<T>(rb, nxm, ntb - 1, ntb, 0, ring, ring_len, rst);
-                    launches += 2;
-                    int rcur = 1, next_g = ntb - 1;
-                    for (int j = 0; j < ntb; j++) {
-                        const int need = ntb - 1 - lag - j;
-                        for (; next_g >= 0 && next_g >= need; next_g--) {
-                            // slot next_g & 1 is free once the adjoint iteration imaging step next_g + 2 is done
-                            TRY(cudaStreamWaitEvent(rst, ev_adj[next_g & 1], 0));
-                            fwi::launch_rebuild_step<T>(rb, nxm, next_g, ntb, rcur, ring, ring_len, next_g & 1, rst);
-                            TRY(cudaEventRecord(ev_reb[next_g & 1], rst));
-                            rcur ^= 1;
-                            launches += sizeof(T) == 4 ? 1 : 2;
-                        }
-                        if (need >= 0) TRY(cudaStreamWaitEvent(st, ev_reb[need & 1], 0));
-                        fwi::StepStreams sst = ss;
-                        sample(1, j, sst);
-                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, need >= 0 ? need - (need & 1) : 0,
-                                                    sst);
-                        if (need >= 0) TRY(cudaEventRecord(ev_adj[need & 1], st));
-                        cur ^= 1;
-                        zsel ^= 1;
-                        launches += kps;
-                    }
-                    // the main stream is past every rebuild: the last adjoint iteration with an
-                    // image waited for it; join the rebuild stream all the same
-                    TRY(cudaEventRecord(ev_reb[0], rst));
-                    TRY(cudaStreamWaitEvent(st, ev_reb[0], 0));
-                    TRY_LAUNCH();
-                } else if (!ckpt) {
-                    for (int j = 0; j < ntb; j++) {
-                        fwi::StepStreams sst = ss;
-                        sample(1, j, sst);
-                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, sst);
-                        cur ^= 1;
-                        zsel ^= 1;
-                    }
-                    TRY_LAUNCH();
-                    launches += kps * ntb;
-                } else {
-                    // segments from the last: recompute its images from the checkpoint, then
-                    // run the adjoint iterations that image inside it
-                    const int lag = exact ? 0 : 1;
-                    Batch<T> rb = b;
-                    // frames of the recompute levels stay zero: never written by the steps
-                    for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
-                    for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
-                    for (int k = 0; k < 4; k++) rb.cp[k] = rcp[k];
-                    rb.tma = use_tma ? (const void *)&rmaps : nullptr;
-                    // `rec` holds the residuals now; the recomputed traces go to the spent obs copy
-                    rb.rec = obs;
-                    // segment seg's images go to half seg & 1 of the image buffer; the
-                    // recompute of segment seg - 1 (on rss) overlaps the adjoint iterations
-                    // imaging inside segment seg (on ss)
-                    TRY(cudaEventRecord(ev_rfork, st));
-                    TRY(cudaStreamWaitEvent(rst, ev_rfork, 0));
-                    auto recompute = [&](int seg) -> int {
-                        const int a = seg * ck_every, e = std::min(a + ck_every, ntb), h = seg & 1;
-                        TRY(cudaStreamWaitEvent(rst, ev_adj[h], 0));  // half h consumed (segment seg + 2)
-                        int rcur = a & 1;
-                        int rc2 = restore_checkpoint(seg, nb, rcur, rst);
-                        if (rc2) return rc2;
-                        for (int g = a; g < e; g++) {
-                            fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, (g - a) + h * ck_every, exact, rss);
-                            rcur ^= 1;
-                        }
-                        TRY(cudaEventRecord(ev_reb[h], rst));
-                        launches += kps * (e - a);
-                        return FWI_OK;
-                    };
-                    const int last = (ntb - 1) / ck_every;
-                    int rc3 = recompute(last);
-                    if (rc3) return rc3;
-                    int j = 0;
-                    for (int seg = last; seg >= 0; seg--) {
-                        const int a = seg * ck_every, h = seg & 1;
-                        if (seg > 0 && (rc3 = recompute(seg - 1))) return rc3;
-                        TRY(cudaStreamWaitEvent(st, ev_reb[h], 0));
-                        for (; j < ntb && ntb - 1 - lag - j >= a; j++) {
+                rc = run_section(section_key(1), 1, nsamp, spts[1], [&]() -> int {
+                    for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+                    for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
+                    for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
+                    int cur = 0;
+                    int zsel = 0;
+                    // image halves the adjoint consumed in this section (an event of an
+                    // earlier batch is complete: that batch ended in a synchronize)
+                    bool consumed[2] = {false, false};
+                    if (bnd) {
+                        // rebuild the CPML-free region backwards one step ahead of the adjoint
+                        // iteration that images it (image slot 0 holds the step just rebuilt)
+                        const int lag = exact ? 0 : 1;
+                        Batch<T> rb = b;
+                        for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
+                        rb.tma = use_tma ? (const void *)&rmaps : nullptr;
+                        // the rebuild stream starts after everything issued so far (the final state copies)
+                        TRY(cudaEventRecord(ev_rfork, st));
+                        TRY(cudaStreamWaitEvent(rst, ev_rfork, 0));
+                        fwi::launch_rebuild_begin<T>(rb, nxm, ntb - 1, ntb, 0, ring, ring_len, rst);
+                        launches += 2;
+                        int rcur = 1, next_g = ntb - 1;
+                        for (int j = 0; j < ntb; j++) {
+                            const int need = ntb - 1 - lag - j;
+                            for (; next_g >= 0 && next_g >= need; next_g--) {
+                                // slot next_g & 1 is free once the adjoint iteration imaging step next_g + 2 is done
+                                if (consumed[next_g & 1]) TRY(cudaStreamWaitEvent(rst, ev_adj[next_g & 1], 0));
+                                fwi::launch_rebuild_step<T>(rb, nxm, next_g, ntb, rcur, ring, ring_len, next_g & 1, rst);
+                                TRY(cudaEventRecord(ev_reb[next_g & 1], rst));
+                                rcur ^= 1;
+                                launches += sizeof(T) == 4 ? 1 : 2;
+                            }
+                            if (need >= 0) TRY(cudaStreamWaitEvent(st, ev_reb[need & 1], 0));
                             fwi::StepStreams sst = ss;
                             sample(1, j, sst);
-                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a - h * ck_every, sst);
+                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, need >= 0 ? need - (need & 1) : 0,
+                                                        sst);
+                            if (need >= 0) {
+                                TRY(cudaEventRecord(ev_adj[need & 1], st));
+                                consumed[need & 1] = true;
+                            }
                             cur ^= 1;
                             zsel ^= 1;
                             launches += kps;
                         }
-                        TRY(cudaEventRecord(ev_adj[h], st));
+                        // the main stream is past every rebuild: the last adjoint iteration with an
+                        // image waited for it; join the rebuild stream all the same
+                        TRY(cudaEventRecord(ev_reb[0], rst));
+                        TRY(cudaStreamWaitEvent(st, ev_reb[0], 0));
+                        TRY_LAUNCH();
+                    } else if (!ckpt) {
+                        for (int j = 0; j < ntb; j++) {
+                            fwi::StepStreams sst = ss;
+                            sample(1, j, sst);
+                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, sst);
+                            cur ^= 1;
+                            zsel ^= 1;
+                        }
+                        TRY_LAUNCH();
+                        launches += kps * ntb;
+                    } else {
+                        // segments from the last: recompute its images from the checkpoint, then
+                        // run the adjoint iterations that image inside it
+                        const int lag = exact ? 0 : 1;
+                        Batch<T> rb = b;
+                        // frames of the recompute levels stay zero: never written by the steps
+                        for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+                        for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
+                        for (int k = 0; k < 4; k++) rb.cp[k] = rcp[k];
+                        rb.tma = use_tma ? (const void *)&rmaps : nullptr;
+                        // `rec` holds the residuals now; the recomputed traces go to the spent obs copy
+                        rb.rec = obs;
+                        // segment seg's images go to half seg & 1 of the image buffer; the
+                        // recompute of segment seg - 1 (on rss) overlaps the adjoint iterations
+                        // imaging inside segment seg (on ss)
+                        TRY(cudaEventRecord(ev_rfork, st));
+                        TRY(cudaStreamWaitEvent(rst, ev_rfork, 0));
+                        auto recompute = [&](int seg) -> int {
+                            const int a = seg * ck_every, e = std::min(a + ck_every, ntb), h = seg & 1;
+                            if (consumed[h]) TRY(cudaStreamWaitEvent(rst, ev_adj[h], 0));  // half h consumed (segment seg + 2)
+                            int rcur = a & 1;
+                            int rc2 = restore_checkpoint(seg, nb, rcur, rst);
+                            if (rc2) return rc2;
+                            for (int g = a; g < e; g++) {
+                                fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, (g - a) + h * ck_every, exact, rss);
+                                rcur ^= 1;
+                            }
+                            TRY(cudaEventRecord(ev_reb[h], rst));
+                            launches += kps * (e - a);
+                            return FWI_OK;
+                        };
+                        const int last = (ntb - 1) / ck_every;
+                        int rc3 = recompute(last);
+                        if (rc3) return rc3;
+                        int j = 0;
+                        for (int seg = last; seg >= 0; seg--) {
+                            const int a = seg * ck_every, h = seg & 1;
+                            if (seg > 0 && (rc3 = recompute(seg - 1))) return rc3;
+                            TRY(cudaStreamWaitEvent(st, ev_reb[h], 0));
+                            for (; j < ntb && ntb - 1 - lag - j >= a; j++) {
+                                fwi::StepStreams sst = ss;
+                                sample(1, j, sst);
+                                fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, a - h * ck_every, sst);
+                                cur ^= 1;
+                                zsel ^= 1;
+                                launches += kps;
+                            }
+                            TRY(cudaEventRecord(ev_adj[h], st));
+                            consumed[h] = true;
+                        }
+                        TRY(cudaEventRecord(ev_reb[0], rst));  // join the recompute stream
+                        TRY(cudaStreamWaitEvent(st, ev_reb[0], 0));
+                        for (; j < ntb; j++) {  // iterations without an image (reference lag)
+                            fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, ss);
+                            cur ^= 1;
+                            zsel ^= 1;
+                            launches += kps;
+                        }
+                        TRY_LAUNCH();
                     }
-                    TRY(cudaEventRecord(ev_reb[0], rst));  // join the recompute stream
-                    TRY(cudaStreamWaitEvent(st, ev_reb[0], 0));
-                    for (; j < ntb; j++) {  // iterations without an image (reference lag)
-                        fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, 0, ss);
-                        cur ^= 1;
-                        zsel ^= 1;
-                        launches += kps;
-                    }
+                    k_accumulate_gradient<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(
+                        grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, nslots, 1, nx, nz, mpitch, pitch, slot);
                     TRY_LAUNCH();
-                }
-                k_accumulate_gradient<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(
-                    grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, nslots, 1, nx, nz, mpitch, pitch, slot);
-                TRY_LAUNCH();
-                launches++;
+                    launches++;
+                    return FWI_OK;
+                });
+                if (rc) return rc;
             }
             TRY(cudaEventRecord(e2, st));
             TRY(cudaEventSynchronize(e2));
@@ -1615,6 +1766,14 @@ int fwi_last_timing(void *ctx, float *out4)
 }
 
 long fwi_last_launches(void *ctx) { return ctx ? as_ctx(ctx)->launches : 0; }
+
+int fwi_set_graphs(void *ctx, int on)
+{
+    if (!ctx) return FWI_ERR_ARG;
+    return as_ctx(ctx)->set_graphs(on != 0);
+}
+
+long fwi_graph_replays(void *ctx) { return ctx ? as_ctx(ctx)->graph_replays : 0; }
 
 long fwi_strip_points(int nx, int nz, int cpml, int *ix, int *iz, long cap)
 {

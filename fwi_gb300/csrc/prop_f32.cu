@@ -72,9 +72,16 @@ template <typename Side, typename Main> void fork_join(const StepStreams &ss, Si
     cudaStreamWaitEvent(ss.side, ss.fork, 0);
     side_work(ss.side);
     cudaEventRecord(ss.join, ss.side);
-    if (ss.t0) cudaEventRecord(ss.t0, ss.main);
+    // timing events: external event nodes when the step is captured into a graph
+    unsigned rec_flags = cudaEventRecordDefault;
+    if (ss.t0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(ss.main, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+            rec_flags = cudaEventRecordExternal;
+        cudaEventRecordWithFlags(ss.t0, ss.main, rec_flags);
+    }
     main_work(ss.main);
-    if (ss.t1) cudaEventRecord(ss.t1, ss.main);
+    if (ss.t1) cudaEventRecordWithFlags(ss.t1, ss.main, rec_flags);
     cudaStreamWaitEvent(ss.main, ss.join, 0);
 }
 

@@ -114,6 +114,8 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_set_tile_timing", [_p, _i])
         _sig(L, "fwi_last_tile_timing", [_p, _p])
         _sig(L, "fwi_last_launches", [_p], _l)
+        _sig(L, "fwi_set_graphs", [_p, _i])
+        _sig(L, "fwi_graph_replays", [_p], _l)
         _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
         _sig(L, "fwi_residual_misfit_noalloc", [_p, _p, _p, _p, _l, _i, _p, _p])
         _sig(L, "fwi_invert_defaults", [C.POINTER(InvertOpts)], None)
@@ -397,8 +399,19 @@ class Context:
         _check(lib().fwi_last_timing(self._h, t.ctypes.data), "fwi_last_timing")
         return t
 
+    def last_cuda_error(self):
+        """The cudaError_t of the last CUDA call that failed in this context (0: none)."""
+        return int(lib().fwi_last_cuda_error(self._h))
+
     def last_launches(self):
         return int(lib().fwi_last_launches(self._h))
+
+    def set_graphs(self, on=True):
+        """CUDA graph replay of repeated batch sections (on by default)."""
+        _check(lib().fwi_set_graphs(self._h, 1 if on else 0), "fwi_set_graphs")
+
+    def graph_replays(self):
+        return int(lib().fwi_graph_replays(self._h))
 
     def set_tile_timing(self, on=True):
         _check(lib().fwi_set_tile_timing(self._h, 1 if on else 0), "fwi_set_tile_timing")

@@ -241,6 +241,19 @@ int fwi_last_tile_timing(void *ctx, double *out4);
 /* How many of this library's kernels the last call launched. */
 long fwi_last_launches(void *ctx);
 
+/* CUDA graphs (no counterpart in the reference, which launches every kernel
+ * from the host).  A batch of fwi_gradient / fwi_misfit / fwi_forward runs as
+ * two sections: the forward steps, and the adjoint with its image rebuild and
+ * the gradient sum.  A section whose launch parameters (batch size, steps,
+ * storage, each shot's steps and window width) repeat is captured into a
+ * CUDA graph the second time and replayed after that: one launch from the
+ * host instead of several per time step, same kernels, same results.  On by
+ * default (environment FWI_GRAPHS=0 at fwi_create: off).  fwi_set_graphs(ctx,
+ * 0) turns it off and frees the graphs; fwi_graph_replays: sections replayed
+ * so far. */
+int fwi_set_graphs(void *ctx, int on);
+long fwi_graph_replays(void *ctx);
+
 /* ---- residual and misfit without device allocation ----
  * No counterpart in the reference (it copies the residual to the host and sums it there,
  * src/main.c:437-454).  For callers that cannot let the library allocate device memory:

@@ -346,3 +346,48 @@ def test_boundary_storage_rebuilds_the_images(exact_case, precision, sprec, tol,
     for a, b in zip(res[0][1:], res[1][1:]):
         assert rel_l2(b[inside], a[inside]) <= tol, rel_l2(b[inside], a[inside])
         assert np.all(np.isfinite(b))
+
+
+@pytest.mark.parametrize("store", ["full", "checkpoint", "boundary"])
+@pytest.mark.parametrize("batch", [2, 1])
+def test_graph_replay_matches_direct_issue_bitwise(exact_case, store, batch):
+    """Batch sections replayed as CUDA graphs (captured on the second call with
+    the same launch parameters) give the results of direct issue bit for bit,
+    with the same launch count and tile-timing samples; batch 1 keys each
+    shot's window and step count separately."""
+    from fwi_gb300 import (Context, MODE_EXACT, PREC_FP32, STORE_BOUNDARY, STORE_CHECKPOINT, STORE_FULL,
+                           make_shots)
+    p, shots, obs, mask, _, _ = exact_case
+    st = dict(full=STORE_FULL, checkpoint=STORE_CHECKPOINT, boundary=STORE_BOUNDARY)[store]
+    ctx = Context(nx=p["nx"], nz=p["nz"], dh=p["dh"], dt=p["dt"], cpml=p["cpml"], f_cpml=p["f"],
+                  nt_max=p["nt"], max_shots=batch, mode=MODE_EXACT, precision=PREC_FP32, store=st, store_prec=1,
+                  ckpt_every=37 if store == "checkpoint" else 0)
+    ctx.set_wavelet(wavelet(p).astype(np.float32))
+    ctx.set_model(*(np.ascontiguousarray(p[k], np.float32) for k in ("vh", "vp", "vn")))
+    ctx.set_tile_timing(True)
+    sh, ob = make_shots(shots), obs.astype(np.float32)
+    runs, launches, tiles = [], [], []
+    for i in range(4):  # direct, captured, replayed, replayed
+        try:
+            runs.append(ctx.gradient(sh, ob, mask))
+        except Exception as e:
+            raise AssertionError(f"call {i}: {e}, cudaError {ctx.last_cuda_error()}") from e
+        launches.append(ctx.last_launches())
+        tiles.append(ctx.last_tile_timing())
+    replays = ctx.graph_replays()
+    traces = [ctx.forward(sh) for _ in range(3)]
+    assert ctx.graph_replays() > replays
+    ctx.set_graphs(False)
+    direct = ctx.gradient(sh, ob, mask)
+    direct_launches = ctx.last_launches()
+    direct_traces = ctx.forward(sh)
+    assert replays == 2 * 2 * (2 // batch)  # two replayed calls x two sections x batches
+    assert len(set(launches)) == 1 and direct_launches == launches[0]
+    for t in tiles[1:]:
+        assert np.all(t[[1, 3]] == tiles[0][[1, 3]]) and np.all(t[[0, 2]] > 0)
+    for r in runs:
+        assert r[0] == direct[0]
+        for a, b in zip(r[1:], direct[1:]):
+            assert np.array_equal(a, b)
+    for t in traces:
+        assert np.array_equal(t, direct_traces)
