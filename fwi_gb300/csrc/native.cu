@@ -458,9 +458,10 @@ struct CtxBase {
     cudaEvent_t tev[2][kTimeSamples][2] = {};
     double tile_ms[2] = {0, 0}, tile_pts[2] = {0, 0};
     long tile_n[2] = {0, 0};
-    // CUDA graphs of the batch sections (Ctx<T>::run_section): on/off, replays so far
+    // CUDA graphs of the batch sections (Ctx<T>::run_section): on/off, sections
+    // replayed and captured
     bool graphs = true;
-    long graph_replays = 0;
+    long graph_replays = 0, graph_captures = 0;
     virtual void drop_sections() {}
     int set_graphs(bool on)
     {
@@ -664,6 +665,7 @@ template <typename T> struct Ctx : CtxBase {
             cudaError_t e = cudaStreamEndCapture(st, &g);
             if (rc == FWI_OK && e == cudaSuccess)
                 e = cudaGraphInstantiateWithFlags(&s->exec, g, cudaGraphInstantiateFlagUseNodePriority);
+            if (rc == FWI_OK && e == cudaSuccess) graph_captures++;
             if (g) cudaGraphDestroy(g);
             if (rc != FWI_OK) return rc;
             if (e != cudaSuccess) {
@@ -1773,7 +1775,14 @@ int fwi_set_graphs(void *ctx, int on)
     return as_ctx(ctx)->set_graphs(on != 0);
 }
 
-long fwi_graph_replays(void *ctx) { return ctx ? as_ctx(ctx)->graph_replays : 0; }
+int fwi_graph_stats(void *ctx, long *out2)
+{
+    if (!ctx || !out2) return FWI_ERR_ARG;
+    const CtxBase *c = as_ctx(ctx);
+    out2[0] = c->graph_replays;
+    out2[1] = c->graph_captures;
+    return FWI_OK;
+}
 
 long fwi_strip_points(int nx, int nz, int cpml, int *ix, int *iz, long cap)
 {

@@ -115,7 +115,7 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_last_tile_timing", [_p, _p])
         _sig(L, "fwi_last_launches", [_p], _l)
         _sig(L, "fwi_set_graphs", [_p, _i])
-        _sig(L, "fwi_graph_replays", [_p], _l)
+        _sig(L, "fwi_graph_stats", [_p, _p])
         _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
         _sig(L, "fwi_residual_misfit_noalloc", [_p, _p, _p, _p, _l, _i, _p, _p])
         _sig(L, "fwi_invert_defaults", [C.POINTER(InvertOpts)], None)
@@ -410,8 +410,14 @@ class Context:
         """CUDA graph replay of repeated batch sections (on by default)."""
         _check(lib().fwi_set_graphs(self._h, 1 if on else 0), "fwi_set_graphs")
 
+    def graph_stats(self):
+        """(sections replayed, sections captured) since creation."""
+        t = np.zeros(2, np.int64)
+        _check(lib().fwi_graph_stats(self._h, t.ctypes.data), "fwi_graph_stats")
+        return tuple(int(v) for v in t)
+
     def graph_replays(self):
-        return int(lib().fwi_graph_replays(self._h))
+        return self.graph_stats()[0]
 
     def set_tile_timing(self, on=True):
         _check(lib().fwi_set_tile_timing(self._h, 1 if on else 0), "fwi_set_tile_timing")

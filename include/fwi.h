@@ -249,10 +249,10 @@ long fwi_last_launches(void *ctx);
  * CUDA graph the second time and replayed after that: one launch from the
  * host instead of several per time step, same kernels, same results.  On by
  * default (environment FWI_GRAPHS=0 at fwi_create: off).  fwi_set_graphs(ctx,
- * 0) turns it off and frees the graphs; fwi_graph_replays: sections replayed
- * so far. */
+ * 0) turns graphs off and frees them.  fwi_graph_stats: out[0] sections
+ * replayed, out[1] sections captured, both since fwi_create. */
 int fwi_set_graphs(void *ctx, int on);
-long fwi_graph_replays(void *ctx);
+int fwi_graph_stats(void *ctx, long *out2);
 
 /* ---- residual and misfit without device allocation ----
  * No counterpart in the reference (it copies the residual to the host and sums it there,

@@ -382,6 +382,7 @@ def test_graph_replay_matches_direct_issue_bitwise(exact_case, store, batch):
     direct_launches = ctx.last_launches()
     direct_traces = ctx.forward(sh)
     assert replays == 2 * 2 * (2 // batch)  # two replayed calls x two sections x batches
+    assert ctx.graph_stats()[1] == 3 * (2 // batch)  # gradient (2) and forward-only (1) sections
     assert len(set(launches)) == 1 and direct_launches == launches[0]
     for t in tiles[1:]:
         assert np.all(t[[1, 3]] == tiles[0][[1, 3]]) and np.all(t[[0, 2]] > 0)
