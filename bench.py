@@ -200,6 +200,8 @@ def native_arm(args, rank, world, dist):
     ctx.forward(shots, out=obs_d)
     ctx.set_model(*w.squared(initial=True))
     g_d = [torch.zeros((w.nz, w.nx), dtype=torch.float32, device="cuda") for _ in range(3)]
+    # launch choice: measured by the autotuner (before the warm-up, untimed) or the built-in one
+    tuning = ctx.autotune(shots, steps=args.autotune) if args.autotune > 0 else None
 
     def step():
         J, *_ = ctx.gradient(shots, obs_d, w.mask, out=g_d)
@@ -272,6 +274,9 @@ def native_arm(args, rank, world, dist):
             "config": {"workload": w.name, "nx": w.nx, "nz": w.nz, "dh": w.dh, "dt": w.dt, "nt": w.nt,
                        "shots": nshots, "receivers_per_shot": nrec, "ricker_hz": w.f, "cpml": w.cpml,
                        "mode": args.mode, "image_store": f"{args.storage}, {args.store}", "batch": args.batch,
+                       "launch_choice": ({k: (round(v, 2) if isinstance(v, float) else v) for k, v in tuning.items()}
+                                         | {"by": f"fwi_autotune, {args.autotune} steps per candidate"}
+                                         if tuning else "built-in"),
                        "l2": f"inputs larger than L2 (observed data {ntr * 4 / 1e6:.0f} MB; the per-step state of "
                              f"all shots {6 * 4 * w.nz * w.nx * nshots / 1e6:.0f} MB; images or rings streamed "
                              f"through HBM)"},
@@ -403,6 +408,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-extras", action="store_true")
+    ap.add_argument("--autotune", type=int, default=48,
+                    help="fwi_autotune with this many steps per candidate before the warm-up (0: built-in choice)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, dist = dist_setup()

@@ -499,6 +499,8 @@ struct CtxBase {
     virtual int set_frequency(float, int) = 0;
     virtual int run(const fwi_shot *, int, const void *, const unsigned char *, void *, void *, void *,
                     double *, void *traces, bool grad) = 0;
+    virtual int autotune(const fwi_shot *, int, int, fwi_tuning *) = 0;
+    virtual int set_tuning(const fwi_shot *, int, const fwi_tuning *) = 0;
     virtual int first_step(float, float, float) = 0;
     virtual int lbfgs_direction(int, double *) = 0;
     virtual int lbfgs_update(float, float, float, int, int) = 0;
@@ -922,6 +924,62 @@ template <typename T> struct Ctx : CtxBase {
         return (int)std::max(1L, std::min((nb + groups - 1) / groups, 64L));
     }
 
+    // Launch choices of a batch's tile passes: shots per block of the interior
+    // and of the layer tile passes, and whether the layer tiles advance the
+    // CPML memory variables themselves (when the tile grid allows it) or
+    // after the strip pass.  Built-in choices from the rules above, or the
+    // ones fwi_autotune measured for the batch's shape.
+    struct Choice {
+        int sg = 1, sg_layer = 1, inline_strip = 0;
+    };
+    struct Tuned {
+        std::vector<long> key;
+        Choice c;
+    };
+    std::vector<Tuned> tuned;
+
+    // What the fastest choice depends on: shots in the batch, widest window,
+    // one window for all, mode, image store type.
+    std::vector<long> choice_key(const std::vector<DevShot> &bs, int nxm) const
+    {
+        return {(long)bs.size(), (long)nxm, uniform_windows(bs) ? 1L : 0L, (long)cfg.mode, (long)store_type()};
+    }
+
+    Choice default_choice(const std::vector<DevShot> &bs, int nxm) const
+    {
+        Choice c;
+        c.sg = shots_per_group(bs, nxm);
+        fwi::TileGrid tg;
+        if (use_tma && uniform_windows(bs)) tg = fwi::tile_grid(nxm, nz, cfg.cpml);
+        c.inline_strip = tg.inline_strip ? 1 : 0;
+        c.sg_layer = c.sg == 1 ? 1 : layer_shots_per_group((int)bs.size(), nxm, tg.xbase, tg.zbase);
+        return c;
+    }
+
+    Choice choice_for(const std::vector<DevShot> &bs, int nxm) const
+    {
+        const std::vector<long> key = choice_key(bs, nxm);
+        for (const Tuned &t : tuned)
+            if (t.key == key) return t.c;
+        return default_choice(bs, nxm);
+    }
+
+    // Groups of more than one shot need one window for all (default_choice
+    // and the tuner keep to that).
+    void apply_choice(Batch<T> &b, const std::vector<DevShot> &bs, int nxm, const Choice &c) const
+    {
+        b.sg = c.sg;
+        b.sg_layer = c.sg_layer;
+        if (use_tma && uniform_windows(bs)) {  // one tile grid fits every shot
+            const fwi::TileGrid tg = fwi::tile_grid(nxm, nz, cfg.cpml);
+            b.xbase = tg.xbase;
+            b.zbase = tg.zbase;
+            b.inline_strip = tg.inline_strip && c.inline_strip;
+            if (const char *e = getenv("FWI_INLINE_STRIP"))  // 0: the strip pass path (tests)
+                if (atoi(e) == 0) b.inline_strip = 0;
+        }
+    }
+
     // CPML table by distance (src/main.c:48-51: L = CPML dh, d0 = -3 ln R / (2 L), in T)
     int cpml_table()
     {
@@ -1138,16 +1196,7 @@ template <typename T> struct Ctx : CtxBase {
             for (int k = 0; k < 4; k++) TRY(cudaMemsetAsync(cp[k], 0, lb, st));
             TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
             Batch<T> b = batch_view(nb);
-            b.sg = shots_per_group(bs, nxm);
-            if (use_tma && uniform_windows(bs)) {  // one tile grid fits every shot
-                const fwi::TileGrid tg = fwi::tile_grid(nxm, nz, cfg.cpml);
-                b.xbase = tg.xbase;
-                b.zbase = tg.zbase;
-                b.inline_strip = tg.inline_strip;
-                if (const char *e = getenv("FWI_INLINE_STRIP"))  // 0: the strip pass path (tests)
-                    if (atoi(e) == 0) b.inline_strip = 0;
-            }
-            b.sg_layer = b.sg == 1 ? 1 : layer_shots_per_group(nb, nxm, b.xbase, b.zbase);
+            apply_choice(b, bs, nxm, choice_for(bs, nxm));
             const int ngroups = (nb + b.sg - 1) / b.sg;
             // gradient slots in use: the interior groups' and the layer tiles' (same window in all)
             const int nslots = std::max(ngroups, (nb + b.sg_layer - 1) / b.sg_layer);
@@ -1396,6 +1445,183 @@ template <typename T> struct Ctx : CtxBase {
         if (stat & fwi::kStatusTimeout) return FWI_ERR_CUDA;
         if (stat & fwi::kStatusSaturated) return FWI_ERR_NUMERIC;
         if (misfit_out && !std::isfinite(*misfit_out)) return FWI_ERR_NUMERIC;
+        return FWI_OK;
+    }
+
+    // ---------------------------------------------------------------- autotuner
+
+    // For each batch shape the shots form: time `steps` forward steps and
+    // `steps` adjoint steps (the tile passes of the batch's shots, at steps
+    // where they all run) of candidate choices, by coordinate descent from the
+    // built-in choice over the interior shots per block, the layer shots per
+    // block and the CPML path, and record the fastest for later calls.  A
+    // candidate replaces the best so far only if at least 1 % faster.  The
+    // candidates' steps run on the context's own buffers; every call clears
+    // those before use, so results only depend on the choice recorded.
+    int autotune(const fwi_shot *sh, int n, int steps, fwi_tuning *out) override
+    {
+        if (!have_model || !have_wavelet) return FWI_ERR_STATE;
+        if (!sh || n <= 0 || steps <= 0) return FWI_ERR_ARG;
+        std::vector<DevShot> all(n);
+        std::vector<long> off(n + 1, 0);
+        for (int k = 0; k < n; k++) {
+            int rc = check_shot(sh[k], all[k]);
+            if (rc) return rc;
+            off[k + 1] = off[k] + (long)all[k].nt * (all[k].rx1 - all[k].rx0);
+        }
+        int rc = refresh_models();
+        if (rc) return rc;
+        const bool exact = cfg.mode == FWI_MODE_EXACT;
+        const bool tiles = sizeof(T) == 4 && use_tma;  // the choices only steer the FP32 tile passes
+        for (int b0 = 0; b0 < n; b0 += B) {
+            const int nb = std::min(B, n - b0);
+            std::vector<DevShot> bs(all.begin() + b0, all.begin() + b0 + nb);
+            int ntb = 0, nxm = 0;
+            for (int k = 0; k < nb; k++) {
+                bs[k].rec_off = off[b0 + k] - off[b0];
+                ntb = std::max(ntb, bs[k].nt);
+                nxm = std::max(nxm, bs[k].nx);
+            }
+            const std::vector<long> key = choice_key(bs, nxm);
+            bool done = false;
+            for (const Tuned &t : tuned) done |= t.key == key;
+            if (done && !(b0 == 0 && out)) continue;
+            TRY(cudaMemcpyAsync(shots, bs.data(), nb * sizeof(DevShot), cudaMemcpyHostToDevice, st));
+            const int K = std::min(steps, ntb);
+            const size_t lb = (size_t)nb * slot * sizeof(T);
+            // device time of one forward + one adjoint step with choice c
+            auto trial = [&](const Choice &c, double &us) -> int {
+                for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
+                for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
+                TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
+                Batch<T> b = batch_view(nb);
+                apply_choice(b, bs, nxm, c);
+                TRY(cudaEventRecord(ev[1], st));
+                int cur = 0;
+                for (int g = ntb - K; g < ntb; g++) {  // every shot runs at the last steps
+                    const int img = cfg.store == FWI_STORE_FULL ? g
+                                    : cfg.store == FWI_STORE_CHECKPOINT ? g % n_img : -1;
+                    fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, img, exact, ss);
+                    cur ^= 1;
+                }
+                cur = 0;
+                int zsel = 0;
+                const int lag = exact ? 0 : 1;
+                for (int j = 0; j < K; j++) {  // ... and at the first adjoint iterations
+                    const int img_g = std::max(0, ntb - 1 - lag - j);
+                    const int base = cfg.store == FWI_STORE_FULL ? 0 : img_g - img_g % n_img;
+                    fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, base, ss);
+                    cur ^= 1;
+                    zsel ^= 1;
+                }
+                TRY_LAUNCH();
+                TRY(cudaEventRecord(ev[2], st));
+                TRY(cudaEventSynchronize(ev[2]));
+                float ms = 0;
+                TRY(cudaEventElapsedTime(&ms, ev[1], ev[2]));
+                us = 1e3 * ms / K;
+                return FWI_OK;
+            };
+            const Choice dflt = default_choice(bs, nxm);
+            Choice best = dflt;
+            double t_best = 0, t_dflt = 0, t = 0;
+            int trials = 0;
+            if ((rc = trial(dflt, t))) return rc;  // warm-up
+            if ((rc = trial(dflt, t_dflt))) return rc;
+            t_best = t_dflt;
+            trials++;
+            auto consider = [&](Choice c) -> int {
+                if (c.sg == best.sg && c.sg_layer == best.sg_layer && c.inline_strip == best.inline_strip) return FWI_OK;
+                int r = trial(c, t);
+                if (r) return r;
+                trials++;
+                if (t < 0.99 * t_best) {
+                    best = c;
+                    t_best = t;
+                }
+                return FWI_OK;
+            };
+            if (tiles && uniform_windows(bs)) {  // groups of several shots need one window
+                const int cand[] = {1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 24, 32, 48, 64};
+                const fwi::TileGrid tg = fwi::tile_grid(nxm, nz, cfg.cpml);
+                for (int pass = 0; pass < 2; pass++) {
+                    for (int v : cand)
+                        if (v <= nb) {
+                            Choice c = best;
+                            c.sg = v;
+                            if ((rc = consider(c))) return rc;
+                        }
+                    for (int v : cand)
+                        if (v <= nb) {
+                            Choice c = best;
+                            c.sg_layer = v;
+                            if ((rc = consider(c))) return rc;
+                        }
+                    if (tg.inline_strip) {
+                        Choice c = best;
+                        c.inline_strip = !c.inline_strip;
+                        if ((rc = consider(c))) return rc;
+                    }
+                }
+            }
+            bool stored = false;
+            for (Tuned &tu : tuned)
+                if (tu.key == key) {
+                    tu.c = best;
+                    stored = true;
+                }
+            if (!stored) tuned.push_back({key, best});
+            if (b0 == 0 && out) {
+                out->shots_per_group = best.sg;
+                out->layer_shots_per_group = best.sg_layer;
+                out->inline_strip = best.inline_strip;
+                out->trials = trials;
+                out->step_us = t_best;
+                out->default_step_us = t_dflt;
+            }
+        }
+        TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));  // candidates ran on stale inputs
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    // Records choice t for the batch shapes the shots form.
+    int set_tuning(const fwi_shot *sh, int n, const fwi_tuning *t) override
+    {
+        if (!sh || n <= 0 || !t) return FWI_ERR_ARG;
+        Choice c;
+        c.sg = t->shots_per_group;
+        c.sg_layer = t->layer_shots_per_group;
+        c.inline_strip = t->inline_strip ? 1 : 0;
+        if (c.sg < 1 || c.sg > 64 || c.sg_layer < 1 || c.sg_layer > 64) return FWI_ERR_ARG;
+        std::vector<DevShot> all(n);
+        for (int k = 0; k < n; k++) {
+            int rc = check_shot(sh[k], all[k]);
+            if (rc) return rc;
+        }
+        std::vector<std::pair<std::vector<long>, Choice>> add;
+        for (int b0 = 0; b0 < n; b0 += B) {
+            const int nb = std::min(B, n - b0);
+            std::vector<DevShot> bs(all.begin() + b0, all.begin() + b0 + nb);
+            int nxm = 0;
+            for (const DevShot &d : bs) nxm = std::max(nxm, d.nx);
+            Choice cb = c;
+            if (!(sizeof(T) == 4 && use_tma && uniform_windows(bs))) {
+                // several windows (or no tile passes): one shot per block
+                if (c.sg != 1 || c.sg_layer != 1) return FWI_ERR_ARG;
+                cb.inline_strip = 0;
+            }
+            add.emplace_back(choice_key(bs, nxm), cb);
+        }
+        for (auto &a : add) {
+            bool stored = false;
+            for (Tuned &tu : tuned)
+                if (tu.key == a.first) {
+                    tu.c = a.second;
+                    stored = true;
+                }
+            if (!stored) tuned.push_back({a.first, a.second});
+        }
         return FWI_OK;
     }
 
@@ -1768,6 +1994,18 @@ int fwi_last_timing(void *ctx, float *out4)
 }
 
 long fwi_last_launches(void *ctx) { return ctx ? as_ctx(ctx)->launches : 0; }
+
+int fwi_autotune(void *ctx, const fwi_shot *shots, int nshots, int steps, fwi_tuning *out)
+{
+    if (!ctx) return FWI_ERR_ARG;
+    return as_ctx(ctx)->autotune(shots, nshots, steps, out);
+}
+
+int fwi_set_tuning(void *ctx, const fwi_shot *shots, int nshots, const fwi_tuning *t)
+{
+    if (!ctx) return FWI_ERR_ARG;
+    return as_ctx(ctx)->set_tuning(shots, nshots, t);
+}
 
 int fwi_set_graphs(void *ctx, int on)
 {

@@ -59,6 +59,11 @@ class InvertOpts(C.Structure):
                 ("flag_min", C.c_int), ("flag_max", C.c_int), ("armijo_c1", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("shots_per_group", C.c_int), ("layer_shots_per_group", C.c_int), ("inline_strip", C.c_int),
+                ("trials", C.c_int), ("step_us", C.c_double), ("default_step_us", C.c_double)]
+
+
 # int (*)(void *user, int band, float f, const void **obs)
 BandObsFn = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_float, C.POINTER(C.c_void_p))
 
@@ -114,6 +119,8 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_set_tile_timing", [_p, _i])
         _sig(L, "fwi_last_tile_timing", [_p, _p])
         _sig(L, "fwi_last_launches", [_p], _l)
+        _sig(L, "fwi_autotune", [_p, shotp, _i, _i, C.POINTER(Tuning)])
+        _sig(L, "fwi_set_tuning", [_p, shotp, _i, C.POINTER(Tuning)])
         _sig(L, "fwi_set_graphs", [_p, _i])
         _sig(L, "fwi_graph_stats", [_p, _p])
         _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
@@ -405,6 +412,18 @@ class Context:
 
     def last_launches(self):
         return int(lib().fwi_last_launches(self._h))
+
+    def autotune(self, shots, steps=48):
+        """Times candidate launch choices per batch shape of `shots` and keeps the fastest
+        (fwi_autotune); returns the first batch's choice and step times."""
+        t = Tuning()
+        _check(lib().fwi_autotune(self._h, shots, len(shots), int(steps), C.byref(t)), "fwi_autotune")
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+    def set_tuning(self, shots, choice):
+        """Records a launch choice (a dict as autotune returns) for the batch shapes of `shots`."""
+        t = Tuning(**{f: choice[f] for f in ("shots_per_group", "layer_shots_per_group", "inline_strip")})
+        _check(lib().fwi_set_tuning(self._h, shots, len(shots), C.byref(t)), "fwi_set_tuning")
 
     def set_graphs(self, on=True):
         """CUDA graph replay of repeated batch sections (on by default)."""
