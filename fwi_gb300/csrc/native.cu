@@ -929,12 +929,19 @@ template <typename T> struct Ctx : CtxBase {
     // CPML memory variables themselves (when the tile grid allows it) or
     // after the strip pass.  Built-in choices from the rules above, or the
     // ones fwi_autotune measured for the batch's shape.
-    struct Choice {
+    struct Choice {  // of one phase (forward or adjoint)
         int sg = 1, sg_layer = 1, inline_strip = 0;
+        bool operator==(const Choice &o) const
+        {
+            return sg == o.sg && sg_layer == o.sg_layer && inline_strip == o.inline_strip;
+        }
+    };
+    struct Choices {  // the two phases share no state that depends on it
+        Choice fwd, adj;
     };
     struct Tuned {
         std::vector<long> key;
-        Choice c;
+        Choices c;
     };
     std::vector<Tuned> tuned;
 
@@ -956,12 +963,23 @@ template <typename T> struct Ctx : CtxBase {
         return c;
     }
 
-    Choice choice_for(const std::vector<DevShot> &bs, int nxm) const
+    Choices choice_for(const std::vector<DevShot> &bs, int nxm) const
     {
         const std::vector<long> key = choice_key(bs, nxm);
         for (const Tuned &t : tuned)
             if (t.key == key) return t.c;
-        return default_choice(bs, nxm);
+        const Choice d = default_choice(bs, nxm);
+        return {d, d};
+    }
+
+    void record_choice(const std::vector<long> &key, const Choices &c)
+    {
+        for (Tuned &t : tuned)
+            if (t.key == key) {
+                t.c = c;
+                return;
+            }
+        tuned.push_back({key, c});
     }
 
     // Groups of more than one shot need one window for all (default_choice
@@ -1195,8 +1213,12 @@ template <typename T> struct Ctx : CtxBase {
             for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
             for (int k = 0; k < 4; k++) TRY(cudaMemsetAsync(cp[k], 0, lb, st));
             TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
+            // the adjoint's view (its groups own the gradient slots) and the forward's
+            const Choices ch = choice_for(bs, nxm);
             Batch<T> b = batch_view(nb);
-            apply_choice(b, bs, nxm, choice_for(bs, nxm));
+            apply_choice(b, bs, nxm, ch.adj);
+            Batch<T> bf = b;
+            apply_choice(bf, bs, nxm, ch.fwd);
             const int ngroups = (nb + b.sg - 1) / b.sg;
             // gradient slots in use: the interior groups' and the layer tiles' (same window in all)
             const int nslots = std::max(ngroups, (nb + b.sg_layer - 1) / b.sg_layer);
@@ -1227,6 +1249,7 @@ template <typename T> struct Ctx : CtxBase {
             auto section_key = [&](long tag) {
                 std::vector<long> k = {tag, nb, ntb, nxm, exact, want_grad, ckpt, bnd, ck_every, timed, tstride,
                                        nslots};
+                key_batch(k, bf);  // the adjoint section's segment recompute runs forward steps
                 key_batch(k, b);
                 for (const DevShot &d : bs) {
                     k.push_back(d.nt);
@@ -1243,8 +1266,8 @@ template <typename T> struct Ctx : CtxBase {
                     }
                     fwi::StepStreams sst = ss;
                     sample(0, g, sst);
-                    if (bnd) fwi::launch_save_ring<T>(b, nxm, g, ntb, cur, ring, ring_len, st);
-                    fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, (want_grad && !ckpt && !bnd) ? g : -1, exact,
+                    if (bnd) fwi::launch_save_ring<T>(bf, nxm, g, ntb, cur, ring, ring_len, st);
+                    fwi::launch_forward_step<T>(bf, nxm, g, ntb, cur, (want_grad && !ckpt && !bnd) ? g : -1, exact,
                                                 sst);
                     cur ^= 1;
                 }
@@ -1338,7 +1361,7 @@ template <typename T> struct Ctx : CtxBase {
                         // segments from the last: recompute its images from the checkpoint, then
                         // run the adjoint iterations that image inside it
                         const int lag = exact ? 0 : 1;
-                        Batch<T> rb = b;
+                        Batch<T> rb = bf;  // forward steps: the forward's choice
                         // frames of the recompute levels stay zero: never written by the steps
                         for (auto &p : rlvl) TRY(cudaMemsetAsync(p, 0, lb, st));
                         for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
@@ -1489,30 +1512,29 @@ template <typename T> struct Ctx : CtxBase {
             TRY(cudaMemcpyAsync(shots, bs.data(), nb * sizeof(DevShot), cudaMemcpyHostToDevice, st));
             const int K = std::min(steps, ntb);
             const size_t lb = (size_t)nb * slot * sizeof(T);
-            // device time of one forward + one adjoint step with choice c
-            auto trial = [&](const Choice &c, double &us) -> int {
+            // device time per step of phase ph (0 forward, 1 adjoint) with choice c
+            auto trial = [&](const Choice &c, int ph, double &us) -> int {
                 for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
                 for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
                 TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
                 Batch<T> b = batch_view(nb);
                 apply_choice(b, bs, nxm, c);
                 TRY(cudaEventRecord(ev[1], st));
-                int cur = 0;
-                for (int g = ntb - K; g < ntb; g++) {  // every shot runs at the last steps
-                    const int img = cfg.store == FWI_STORE_FULL ? g
-                                    : cfg.store == FWI_STORE_CHECKPOINT ? g % n_img : -1;
-                    fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, img, exact, ss);
-                    cur ^= 1;
-                }
-                cur = 0;
-                int zsel = 0;
+                int cur = 0, zsel = 0;
                 const int lag = exact ? 0 : 1;
-                for (int j = 0; j < K; j++) {  // ... and at the first adjoint iterations
-                    const int img_g = std::max(0, ntb - 1 - lag - j);
-                    const int base = cfg.store == FWI_STORE_FULL ? 0 : img_g - img_g % n_img;
-                    fwi::launch_adjoint_step<T>(b, nxm, j, ntb, cur, zsel, exact, base, ss);
+                for (int k = 0; k < K; k++) {
+                    if (ph == 0) {  // every shot runs at the last steps
+                        const int g = ntb - K + k;
+                        const int img = cfg.store == FWI_STORE_FULL ? g
+                                        : cfg.store == FWI_STORE_CHECKPOINT ? g % n_img : -1;
+                        fwi::launch_forward_step<T>(b, nxm, g, ntb, cur, img, exact, ss);
+                    } else {  // ... and at the first adjoint iterations
+                        const int img_g = std::max(0, ntb - 1 - lag - k);
+                        const int base = cfg.store == FWI_STORE_FULL ? 0 : img_g - img_g % n_img;
+                        fwi::launch_adjoint_step<T>(b, nxm, k, ntb, cur, zsel, exact, base, ss);
+                        zsel ^= 1;
+                    }
                     cur ^= 1;
-                    zsel ^= 1;
                 }
                 TRY_LAUNCH();
                 TRY(cudaEventRecord(ev[2], st));
@@ -1523,61 +1545,63 @@ template <typename T> struct Ctx : CtxBase {
                 return FWI_OK;
             };
             const Choice dflt = default_choice(bs, nxm);
-            Choice best = dflt;
-            double t_best = 0, t_dflt = 0, t = 0;
+            Choices best{dflt, dflt};
+            double t_best[2] = {0, 0}, t_dflt[2] = {0, 0}, t = 0;
             int trials = 0;
-            if ((rc = trial(dflt, t))) return rc;  // warm-up
-            if ((rc = trial(dflt, t_dflt))) return rc;
-            t_best = t_dflt;
-            trials++;
-            auto consider = [&](Choice c) -> int {
-                if (c.sg == best.sg && c.sg_layer == best.sg_layer && c.inline_strip == best.inline_strip) return FWI_OK;
-                int r = trial(c, t);
-                if (r) return r;
+            for (int ph = 0; ph < 2; ph++) {
+                if ((rc = trial(dflt, ph, t))) return rc;  // warm-up
+                if ((rc = trial(dflt, ph, t_dflt[ph]))) return rc;
+                t_best[ph] = t_dflt[ph];
                 trials++;
-                if (t < 0.99 * t_best) {
-                    best = c;
-                    t_best = t;
-                }
-                return FWI_OK;
-            };
-            if (tiles && uniform_windows(bs)) {  // groups of several shots need one window
+                Choice &bp = ph == 0 ? best.fwd : best.adj;
+                auto consider = [&](const Choice &c) -> int {
+                    if (c == bp) return FWI_OK;
+                    const int r = trial(c, ph, t);
+                    if (r) return r;
+                    trials++;
+                    if (t < 0.99 * t_best[ph]) {
+                        bp = c;
+                        t_best[ph] = t;
+                    }
+                    return FWI_OK;
+                };
+                if (!(tiles && uniform_windows(bs))) continue;  // groups of several shots need one window
                 const int cand[] = {1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 24, 32, 48, 64};
                 const fwi::TileGrid tg = fwi::tile_grid(nxm, nz, cfg.cpml);
                 for (int pass = 0; pass < 2; pass++) {
                     for (int v : cand)
                         if (v <= nb) {
-                            Choice c = best;
+                            Choice c = bp;
                             c.sg = v;
                             if ((rc = consider(c))) return rc;
                         }
                     for (int v : cand)
                         if (v <= nb) {
-                            Choice c = best;
+                            Choice c = bp;
                             c.sg_layer = v;
                             if ((rc = consider(c))) return rc;
                         }
                     if (tg.inline_strip) {
-                        Choice c = best;
+                        Choice c = bp;
                         c.inline_strip = !c.inline_strip;
                         if ((rc = consider(c))) return rc;
                     }
                 }
             }
-            bool stored = false;
-            for (Tuned &tu : tuned)
-                if (tu.key == key) {
-                    tu.c = best;
-                    stored = true;
-                }
-            if (!stored) tuned.push_back({key, best});
+            record_choice(key, best);
             if (b0 == 0 && out) {
-                out->shots_per_group = best.sg;
-                out->layer_shots_per_group = best.sg_layer;
-                out->inline_strip = best.inline_strip;
+                for (int ph = 0; ph < 2; ph++) {
+                    const Choice &c = ph == 0 ? best.fwd : best.adj;
+                    fwi_phase_choice &o = ph == 0 ? out->forward : out->adjoint;
+                    o.shots_per_group = c.sg;
+                    o.layer_shots_per_group = c.sg_layer;
+                    o.inline_strip = c.inline_strip;
+                }
                 out->trials = trials;
-                out->step_us = t_best;
-                out->default_step_us = t_dflt;
+                out->forward_us = t_best[0];
+                out->adjoint_us = t_best[1];
+                out->default_forward_us = t_dflt[0];
+                out->default_adjoint_us = t_dflt[1];
             }
         }
         TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));  // candidates ran on stale inputs
@@ -1589,39 +1613,37 @@ template <typename T> struct Ctx : CtxBase {
     int set_tuning(const fwi_shot *sh, int n, const fwi_tuning *t) override
     {
         if (!sh || n <= 0 || !t) return FWI_ERR_ARG;
-        Choice c;
-        c.sg = t->shots_per_group;
-        c.sg_layer = t->layer_shots_per_group;
-        c.inline_strip = t->inline_strip ? 1 : 0;
-        if (c.sg < 1 || c.sg > 64 || c.sg_layer < 1 || c.sg_layer > 64) return FWI_ERR_ARG;
+        Choices c;
+        for (int ph = 0; ph < 2; ph++) {
+            const fwi_phase_choice &i = ph == 0 ? t->forward : t->adjoint;
+            Choice &o = ph == 0 ? c.fwd : c.adj;
+            o.sg = i.shots_per_group;
+            o.sg_layer = i.layer_shots_per_group;
+            o.inline_strip = i.inline_strip ? 1 : 0;
+            if (o.sg < 1 || o.sg > 64 || o.sg_layer < 1 || o.sg_layer > 64) return FWI_ERR_ARG;
+        }
         std::vector<DevShot> all(n);
         for (int k = 0; k < n; k++) {
             int rc = check_shot(sh[k], all[k]);
             if (rc) return rc;
         }
-        std::vector<std::pair<std::vector<long>, Choice>> add;
+        std::vector<std::pair<std::vector<long>, Choices>> add;
         for (int b0 = 0; b0 < n; b0 += B) {
             const int nb = std::min(B, n - b0);
             std::vector<DevShot> bs(all.begin() + b0, all.begin() + b0 + nb);
             int nxm = 0;
             for (const DevShot &d : bs) nxm = std::max(nxm, d.nx);
-            Choice cb = c;
+            Choices cb = c;
             if (!(sizeof(T) == 4 && use_tma && uniform_windows(bs))) {
                 // several windows (or no tile passes): one shot per block
-                if (c.sg != 1 || c.sg_layer != 1) return FWI_ERR_ARG;
-                cb.inline_strip = 0;
+                for (Choice *o : {&cb.fwd, &cb.adj}) {
+                    if (o->sg != 1 || o->sg_layer != 1) return FWI_ERR_ARG;
+                    o->inline_strip = 0;
+                }
             }
             add.emplace_back(choice_key(bs, nxm), cb);
         }
-        for (auto &a : add) {
-            bool stored = false;
-            for (Tuned &tu : tuned)
-                if (tu.key == a.first) {
-                    tu.c = a.second;
-                    stored = true;
-                }
-            if (!stored) tuned.push_back({a.first, a.second});
-        }
+        for (auto &a : add) record_choice(a.first, a.second);
         return FWI_OK;
     }
 

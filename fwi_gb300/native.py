@@ -59,9 +59,14 @@ class InvertOpts(C.Structure):
                 ("flag_min", C.c_int), ("flag_max", C.c_int), ("armijo_c1", C.c_double)]
 
 
+class PhaseChoice(C.Structure):
+    _fields_ = [("shots_per_group", C.c_int), ("layer_shots_per_group", C.c_int), ("inline_strip", C.c_int)]
+
+
 class Tuning(C.Structure):
-    _fields_ = [("shots_per_group", C.c_int), ("layer_shots_per_group", C.c_int), ("inline_strip", C.c_int),
-                ("trials", C.c_int), ("step_us", C.c_double), ("default_step_us", C.c_double)]
+    _fields_ = [("forward", PhaseChoice), ("adjoint", PhaseChoice), ("trials", C.c_int),
+                ("forward_us", C.c_double), ("adjoint_us", C.c_double),
+                ("default_forward_us", C.c_double), ("default_adjoint_us", C.c_double)]
 
 
 # int (*)(void *user, int band, float f, const void **obs)
@@ -418,11 +423,18 @@ class Context:
         (fwi_autotune); returns the first batch's choice and step times."""
         t = Tuning()
         _check(lib().fwi_autotune(self._h, shots, len(shots), int(steps), C.byref(t)), "fwi_autotune")
-        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+        out = {f: getattr(t, f) for f, _ in Tuning._fields_}
+        for ph in ("forward", "adjoint"):
+            out[ph] = {f: getattr(out[ph], f) for f, _ in PhaseChoice._fields_}
+        return out
 
     def set_tuning(self, shots, choice):
-        """Records a launch choice (a dict as autotune returns) for the batch shapes of `shots`."""
-        t = Tuning(**{f: choice[f] for f in ("shots_per_group", "layer_shots_per_group", "inline_strip")})
+        """Records a launch choice ({"forward": {...}, "adjoint": {...}} as autotune returns) for the
+        batch shapes of `shots`."""
+        t = Tuning()
+        for ph in ("forward", "adjoint"):
+            for f, _ in PhaseChoice._fields_:
+                setattr(getattr(t, ph), f, int(choice[ph][f]))
         _check(lib().fwi_set_tuning(self._h, shots, len(shots), C.byref(t)), "fwi_set_tuning")
 
     def set_graphs(self, on=True):

@@ -246,29 +246,34 @@ long fwi_last_launches(void *ctx);
  * shapes their work is how many shots one block takes through the tile (the
  * interior and the layer tile passes separately; more than one needs every
  * shot of the batch on one window) and whether the layer tiles advance the
- * CPML memory variables themselves or after a strip pass.  fwi_autotune times
- * `steps` forward and `steps` adjoint steps of candidate choices for each
- * batch the shots form (coordinate descent from the built-in choice) and
- * records the fastest per batch shape (shots in the batch, widest window, one
- * window or several, mode, image type); later fwi_gradient / fwi_misfit /
- * fwi_forward calls on batches of that shape use it.  Results stay within
- * rounding of the built-in choice's; for a given choice they are
- * deterministic.  `out` (may be NULL): the first batch's choice and its
- * device time per forward + adjoint step, beside the built-in one's.  Time
- * blocking (several steps per pass) is not implemented: one step per pass. */
+ * CPML memory variables themselves or after a strip pass; the forward and
+ * the adjoint are chosen separately.  fwi_autotune times `steps` steps of
+ * candidate choices of each phase for each batch the shots form (coordinate
+ * descent from the built-in choice; a candidate must be 1 % faster to
+ * replace it) and records the fastest per batch shape (shots in the batch,
+ * widest window, one window or several, mode, image type); later
+ * fwi_gradient / fwi_misfit / fwi_forward calls on batches of that shape use
+ * it.  Results stay within FP32 rounding of the built-in choice's; for a
+ * given choice they are deterministic.  `out` (may be NULL): the first
+ * batch's choice and its device time per step, beside the built-in one's.
+ * Time blocking (several steps per pass) is not implemented: one step per
+ * pass. */
 typedef struct {
     int shots_per_group;        /* shots per block, interior tile passes */
     int layer_shots_per_group;  /* shots per block, layer tile passes */
     int inline_strip;           /* 1: layer tiles advance the CPML memory variables; 0: strip pass first */
-    int trials;                 /* candidate choices timed */
-    double step_us;             /* forward + adjoint step with the choice, device time (us) */
-    double default_step_us;     /* the same with the built-in choice */
+} fwi_phase_choice;
+typedef struct {
+    fwi_phase_choice forward, adjoint;
+    int trials;                                   /* candidate runs timed */
+    double forward_us, adjoint_us;                /* device time per step with the choice (us) */
+    double default_forward_us, default_adjoint_us;/* the same with the built-in choice */
 } fwi_tuning;
 int fwi_autotune(void *ctx, const fwi_shot *shots, int nshots, int steps, fwi_tuning *out);
-/* Records t's choice (its first three fields) for the batch shapes the shots
- * form, as fwi_autotune does: a choice tuned once, kept and given again gives
- * the same results bit for bit.  FWI_ERR_ARG when it does not fit: a group
- * size outside 1..64, or above 1 for a batch of several windows. */
+/* Records t's choice (forward, adjoint) for the batch shapes the shots form,
+ * as fwi_autotune does: a choice tuned once, kept and given again gives the
+ * same results bit for bit.  FWI_ERR_ARG when it does not fit: a group size
+ * outside 1..64, or above 1 for a batch of several windows. */
 int fwi_set_tuning(void *ctx, const fwi_shot *shots, int nshots, const fwi_tuning *t);
 
 /* CUDA graphs (no counterpart in the reference, which launches every kernel

@@ -65,9 +65,12 @@ def test_autotune_choice_is_applied_and_reproducible(one_window):
         res.append(ctx.gradient(shots, obs))
         del ctx
     t = tunings[0]
-    assert 1 <= t["shots_per_group"] <= 6 and 1 <= t["layer_shots_per_group"] <= 6
-    assert t["inline_strip"] in (0, 1) and t["trials"] > 1
-    assert 0 < t["step_us"] <= t["default_step_us"]
+    for ph in ("forward", "adjoint"):
+        c = t[ph]
+        assert 1 <= c["shots_per_group"] <= 6 and 1 <= c["layer_shots_per_group"] <= 6
+        assert c["inline_strip"] in (0, 1)
+        assert 0 < t[f"{ph}_us"] <= t[f"default_{ph}_us"]
+    assert t["trials"] > 2
     tuned, given, builtin = res
     assert tuned[0] == given[0]
     for a, b in zip(tuned[1:], given[1:]):
@@ -77,11 +80,16 @@ def test_autotune_choice_is_applied_and_reproducible(one_window):
         assert rel_l2(a, b) <= 1e-5, rel_l2(a, b)
 
 
-@pytest.mark.parametrize("sg,sl,inl", [(1, 1, 0), (2, 6, 1), (6, 1, 0), (3, 2, 1)])
-def test_every_choice_gives_the_same_gradient(one_window, sg, sl, inl):
+def phase(sg, sl, inl):
+    return dict(shots_per_group=sg, layer_shots_per_group=sl, inline_strip=inl)
+
+
+@pytest.mark.parametrize("fwd,adj", [((1, 1, 0), (1, 1, 0)), ((2, 6, 1), (3, 2, 1)), ((6, 1, 0), (6, 1, 0)),
+                                     ((3, 2, 1), (2, 6, 0))])
+def test_every_choice_gives_the_same_gradient(one_window, fwd, adj):
     p, shots, obs = one_window
     out = []
-    for choice in (None, dict(shots_per_group=sg, layer_shots_per_group=sl, inline_strip=inl)):
+    for choice in (None, dict(forward=phase(*fwd), adjoint=phase(*adj))):
         ctx = context(p, 6)
         ctx.set_model(p["vh"], p["vp"], p["vn"])
         if choice:
@@ -102,9 +110,9 @@ def test_several_windows_keep_one_shot_per_block():
     ctx = context(p, 2, max_window=p["nx"])
     ctx.set_model(p["vh"], p["vp"], p["vn"])
     t = ctx.autotune(shots, steps=16)
-    assert (t["shots_per_group"], t["layer_shots_per_group"], t["inline_strip"], t["trials"]) == (1, 1, 0, 1)
+    assert t["forward"] == t["adjoint"] == phase(1, 1, 0) and t["trials"] == 2  # the built-in choice, per phase
     with pytest.raises(FwiError) as e:
-        ctx.set_tuning(shots, dict(shots_per_group=2, layer_shots_per_group=1, inline_strip=0))
+        ctx.set_tuning(shots, dict(forward=phase(1, 1, 0), adjoint=phase(2, 1, 0)))
     assert e.value.status == -1  # FWI_ERR_ARG
     J, *g = ctx.gradient(shots, obs)
     assert np.isfinite(J) and all(np.all(np.isfinite(a)) for a in g)
