@@ -87,6 +87,24 @@ __device__ __forceinline__ void drain_stages_n(uint64_t *bar, int a, int na, int
 }
 __device__ __forceinline__ void drain_stages(uint64_t *bar, int a, int na) { drain_stages_n(bar, a, na, kStages); }
 
+// The interior passes' pipeline: every thread waits for its stage itself
+// (mbar_wait: try_wait suspends the thread in hardware, no block barrier),
+// and the block meets once, at the end of the iteration, where the stage is
+// handed back for its refill.  stage_release: that meeting, agreeing on
+// whether any thread's wait gave up in this iteration (a thread that gave up
+// skips the stage's work); then the status bit, the loads in flight (shots
+// a + 1 .. a + nst - 1) get a bounded time to land, and false.
+__device__ __forceinline__ bool stage_release(bool ok, uint64_t *bar, int a, int na, int nst, unsigned *status)
+{
+    if (!__syncthreads_or(!ok)) return true;
+    if (threadIdx.x == 0) {
+        atomicOr(status, kStatusTimeout);
+        for (int k = a + 1; k < min(a + nst, na); k++) (void)mbar_wait(&bar[k % nst], (k / nst) & 1);
+    }
+    __syncthreads();
+    return false;
+}
+
 __device__ __forceinline__ int active_shots(const Batch<float> &b, int sg, int *act, bool adjoint, int step, int ntb)
 {
     __shared__ int n_s;
@@ -252,13 +270,10 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
             vP = ld4(Pv0 + so + ipt);
             vF = ld4(Fv0 + so + ipt);
         }
-        if (!stage_ready(&bar[a % kStages], (a / kStages) & 1, b.status)) {
-            drain_stages(bar, a, na);
-            return;
-        }
+        const bool ok = mbar_wait(&bar[a % kStages], (a / kStages) & 1);
         const FwdStage &S = stage[a % kStages];
         float lmax = 0.f;
-        if (any) {
+        if (any && ok) {
             float pv[12];
             {
                 const float *row = &S.P[r][c4];
@@ -341,7 +356,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
             }
         }
         if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)act[a] * (b.nt_max + 1) + g + 1]);
-        __syncthreads();  // every thread is done with this stage
+        if (!stage_release(ok, bar, a, na, kStages, b.status)) return;  // every thread is done with this stage
         if (tid == 0 && a + kStages < na) {
             fence_proxy_async();
             issue(a + kStages);
@@ -433,6 +448,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
         const bool in = gx < nx && gz >= 0 && gz < nz;
         MP[rr][cc] = in ? b.mp[(long)gz * b.mpitch + gsh.x0 + gx] : 0.f;
     }
+    __syncthreads();  // the model tiles, before any thread's first U, V (no block barrier before that)
     const int c4 = 4 * (tid & 7), r = tid >> 3;
     const int ix0 = x0 + c4, iz = z0 + r;
     bool m[4];  // interior points
@@ -462,12 +478,10 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                 Vec4Store<SI>::get(img + b.slot + ipt, iH);
             }
         }
-        if (!stage_ready(&bar[a % kAdjStages], (a / kAdjStages) & 1, b.status)) {
-            drain_stages_n(bar, a, na, kAdjStages);
-            return;
-        }
+        const bool ok = mbar_wait(&bar[a % kAdjStages], (a / kAdjStages) & 1);
         const Stage &S = stage[a % kAdjStages];
         // U = dt^2 (v_hor lP + v_nmo lF) on the x-halo tile, V = dt^2 v_po (lP + lF) on the z-halo tile
+        // (from whatever the stage holds if this thread's wait gave up: the iteration is then discarded)
         for (int k = tid; k < TT * (TH / 4); k += kTmaThreads) {
             const int rr = k / (TH / 4), cc = 4 * (k - rr * (TH / 4));
             const float4 p = ld4(&S.P[rr + kRad][cc]), f = ld4(&S.F[rr + kRad][cc]);
@@ -481,10 +495,10 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
             *reinterpret_cast<float4 *>(&V[rr][cc]) =
                 make_float4(v.x * (p.x + f.x), v.y * (p.y + f.y), v.z * (p.z + f.z), v.w * (p.w + f.w));
         }
-        __syncthreads();
+        const bool bad = __syncthreads_or(!ok);  // U and V complete; any thread's wait given up
         const AdjShot &sh = ps[a];
         const long so = sh.so;
-        if (any) {
+        if (any && !bad) {
             float uv[12];
             {
                 const float4 a0 = ld4(&U[r][c4]), a1 = ld4(&U[r][c4 + 4]), a2 = ld4(&U[r][c4 + 8]);
@@ -547,7 +561,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                 }
             }
         }
-        __syncthreads();  // stage, U and V are free again
+        if (!stage_release(!bad, bar, a, na, kAdjStages, b.status)) return;  // stage, U and V are free again
         if (tid == 0 && a + kAdjStages < na) {
             fence_proxy_async();
             issue(a + kAdjStages);
