@@ -1512,15 +1512,35 @@ template <typename T> struct Ctx : CtxBase {
             TRY(cudaMemcpyAsync(shots, bs.data(), nb * sizeof(DevShot), cudaMemcpyHostToDevice, st));
             const int K = std::min(steps, ntb);
             const size_t lb = (size_t)nb * slot * sizeof(T);
-            // device time per step of phase ph (0 forward, 1 adjoint) with choice c
+            const Choice dflt = default_choice(bs, nxm);
+            Choices best{dflt, dflt};
+            // device time per step of phase ph (0 forward, 1 adjoint) with choice c.  The adjoint
+            // steps run beside what runs beside them in a gradient call: with checkpoint storage
+            // the segment recompute (forward steps on the recompute streams, with the forward's
+            // choice), with boundary storage the image rebuild, one step per adjoint step.
             auto trial = [&](const Choice &c, int ph, double &us) -> int {
                 for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
                 for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
                 TRY(cudaMemsetAsync(amax, 0, (size_t)nb * (nt_max + 1) * sizeof(float), st));
                 Batch<T> b = batch_view(nb);
                 apply_choice(b, bs, nxm, c);
+                const bool partner = ph == 1 && cfg.store != FWI_STORE_FULL;
+                const bool recompute = cfg.store == FWI_STORE_CHECKPOINT;
+                Batch<T> rb = batch_view(nb);
+                if (partner) {
+                    apply_choice(rb, bs, nxm, recompute ? best.fwd : c);
+                    for (int k = 0; k < 6; k++) rb.lvl[k] = rlvl[k];
+                    if (recompute)
+                        for (int k = 0; k < 4; k++) rb.cp[k] = rcp[k];
+                    rb.tma = use_tma ? (const void *)&rmaps : nullptr;
+                    rb.rec = obs;
+                }
                 TRY(cudaEventRecord(ev[1], st));
-                int cur = 0, zsel = 0;
+                if (partner) {
+                    TRY(cudaEventRecord(ev_rfork, st));
+                    TRY(cudaStreamWaitEvent(rst, ev_rfork, 0));
+                }
+                int cur = 0, zsel = 0, rcur = 0;
                 const int lag = exact ? 0 : 1;
                 for (int k = 0; k < K; k++) {
                     if (ph == 0) {  // every shot runs at the last steps
@@ -1533,10 +1553,22 @@ template <typename T> struct Ctx : CtxBase {
                         const int base = cfg.store == FWI_STORE_FULL ? 0 : img_g - img_g % n_img;
                         fwi::launch_adjoint_step<T>(b, nxm, k, ntb, cur, zsel, exact, base, ss);
                         zsel ^= 1;
+                        if (partner) {
+                            const int g = ntb - 1 - k;
+                            if (recompute)
+                                fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, g % n_img, exact, rss);
+                            else
+                                fwi::launch_rebuild_step<T>(rb, nxm, g, ntb, rcur, ring, ring_len, g & 1, rst);
+                            rcur ^= 1;
+                        }
                     }
                     cur ^= 1;
                 }
                 TRY_LAUNCH();
+                if (partner) {  // the partner stream joins the timed region's end
+                    TRY(cudaEventRecord(ev_reb[0], rst));
+                    TRY(cudaStreamWaitEvent(st, ev_reb[0], 0));
+                }
                 TRY(cudaEventRecord(ev[2], st));
                 TRY(cudaEventSynchronize(ev[2]));
                 float ms = 0;
@@ -1544,8 +1576,6 @@ template <typename T> struct Ctx : CtxBase {
                 us = 1e3 * ms / K;
                 return FWI_OK;
             };
-            const Choice dflt = default_choice(bs, nxm);
-            Choices best{dflt, dflt};
             double t_best[2] = {0, 0}, t_dflt[2] = {0, 0}, t = 0;
             int trials = 0;
             for (int ph = 0; ph < 2; ph++) {

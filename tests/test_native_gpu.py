@@ -392,3 +392,40 @@ def test_graph_replay_matches_direct_issue_bitwise(exact_case, store, batch):
             assert np.array_equal(a, b)
     for t in traces:
         assert np.array_equal(t, direct_traces)
+
+
+def edge_cases():
+    p = exact_problem(seed=13, nx=64, nz=52, nt=120)
+    nx, nz, nt = p["nx"], p["nz"], p["nt"]
+    return p, {
+        "single receiver": [dict(sx=30, sz=10, rz=12, rx0=40, rx1=41, nt=nt, x0=0, nxw=0)],
+        "first interior row and column": [dict(sx=4, sz=4, rz=4, rx0=4, rx1=9, nt=nt, x0=0, nxw=0)],
+        "last interior column, deep source": [dict(sx=nx - 5, sz=nz - 5, rz=nz - 5, rx0=nx - 9, rx1=nx - 4, nt=nt,
+                                                  x0=0, nxw=0)],
+        "window flush with the right edge": [dict(sx=nx - 12, sz=6, rz=5, rx0=nx - 36, rx1=nx - 4, nt=nt,
+                                                  x0=nx - 40, nxw=40)],
+        "record shorter than the timing sampler": [dict(sx=20, sz=6, rz=5, rx0=4, rx1=nx - 4, nt=6, x0=0, nxw=0)],
+        "batch larger than the shots, two windows": [
+            dict(sx=20, sz=6, rz=5, rx0=4, rx1=nx - 4, nt=nt, x0=0, nxw=0),
+            dict(sx=30, sz=8, rz=6, rx0=14, rx1=50, nt=nt - 20, x0=10, nxw=44),
+            dict(sx=40, sz=7, rz=6, rx0=14, rx1=50, nt=nt - 50, x0=10, nxw=44)],
+    }
+
+
+@pytest.mark.parametrize("case", list(edge_cases()[1]))
+def test_edge_geometries_match_fp64_oracle(case):
+    """FP32 tile path against the FP64 exact-adjoint oracle on edge geometries
+    (tolerances as above: gradients 1e-4, misfit 1e-5), with random observed
+    data so that the residuals are far above the traces' rounding."""
+    from fwi_gb300 import PREC_FP32
+    p, cases = edge_cases()
+    shots = cases[case]
+    rng = np.random.default_rng(5)
+    nobs = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in shots)
+    obs = 1e-3 * rng.standard_normal(nobs)
+    mask = (rng.random(sum(s["rx1"] - s["rx0"] for s in shots)) > 0.1).astype(np.uint8)
+    J, g = oracle_exact(p, shots, obs, mask)
+    _, (Jg, *gg) = run_exact(p, shots, obs, mask, PREC_FP32, batch=len(shots) + 1)
+    assert abs(Jg - J) <= 1e-5 * J
+    for a, b in zip(gg, g):
+        assert rel_l2(a, b) <= 1e-4, rel_l2(a, b)
