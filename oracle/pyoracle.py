@@ -1,8 +1,8 @@
 """ctypes bindings of the CPU oracle (test infrastructure only).
 
 Only tests/, the smoke check in __graft_entry__.py and bench.py's CPU
-baseline / reference arm import this module, as the checker or the timed CPU
-baseline.  The product library never does.
+baseline / reference arm import this module, to check results against it or
+to time it as the CPU baseline.  The product library never does.
 
 `lib()` loads oracle/liboracle.so (the C restatement, vti_oracle.h), building
 it with `make -C oracle` when it is missing.  `ref_lib()` loads

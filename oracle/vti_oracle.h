@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library under
  * fwi_gb300/) links, loads or calls this code; only tests/, the smoke check
  * in __graft_entry__.py and the cpu_baseline / reference arm of bench.py use
- * it, and only as the checker or the timed CPU baseline.
+ * it, and only to check results against it or to time it as the CPU baseline.
  *
  * Two families of functions:
  *
