@@ -44,6 +44,18 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def make_workload(args):
+    """The named seeded workload; --shots and --nt replace its shot count and step count
+    where it has them (C4 draws each shot's steps; its --shots takes the first shots of the set)."""
+    from fwi_gb300 import synth
+    kw = {}
+    if args.shots is not None and args.workload != "C1":
+        kw["shots"] = args.shots
+    if args.nt is not None and args.workload in ("C2", "C3", "C5"):
+        kw["nt"] = args.nt
+    return synth.WORKLOADS[args.workload](**kw)
+
+
 def traffic_from_profile(name):
     path = os.path.join(ROOT, "profiles", name)
     try:
@@ -172,8 +184,7 @@ def native_arm(args, rank, world, dist):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    w = synth.WORKLOADS[args.workload](shots=args.shots, nt=args.nt) if args.workload in ("C2", "C3") \
-        else synth.WORKLOADS[args.workload]()
+    w = make_workload(args)
     shots = fwi_gb300.make_shots(w.shots)
     mode = fwi_gb300.MODE_EXACT if args.mode == "exact" else fwi_gb300.MODE_REF_COMPAT
     sprec = {"fp32": fwi_gb300.SPREC_NATIVE, "fp16": fwi_gb300.SPREC_FP16, "bf16": fwi_gb300.SPREC_BF16}[args.store]
@@ -377,9 +388,7 @@ def reference_arm(args, rank, world, dist):
     path of its own), all host threads, bounded samples of the same workload."""
     if rank != 0:
         return None
-    from fwi_gb300 import synth
-    w = synth.WORKLOADS[args.workload](shots=args.shots, nt=args.nt) if args.workload in ("C2", "C3") \
-        else synth.WORKLOADS[args.workload]()
+    w = make_workload(args)
     secs = max(2.0, args.cpu_seconds / max(1, args.steps))
     vals = []
     for _ in range(args.warmup):  # untimed, short samples
@@ -407,8 +416,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="C2")
-    ap.add_argument("--shots", type=int, default=32)
-    ap.add_argument("--nt", type=int, default=3000)
+    ap.add_argument("--shots", type=int, default=None, help="shots (default: the workload's own)")
+    ap.add_argument("--nt", type=int, default=None, help="time steps (default: the workload's own)")
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--mode", default="exact", choices=["exact", "ref"])
     ap.add_argument("--store", default="fp16", choices=["fp32", "fp16", "bf16"])

@@ -606,7 +606,7 @@ template <typename T> struct Ctx : CtxBase {
     {
         for (long v : {(long)b.B, (long)b.nz, (long)b.pitch, (long)b.mpitch, (long)b.cpml, (long)b.nt_max, b.slot,
                        (long)b.store_type, (long)b.n_img, (long)b.sg, (long)b.sg_layer, (long)b.xbase, (long)b.zbase,
-                       (long)b.inline_strip})
+                       (long)b.inline_strip, (long)b.mixed})
             key_add(k, v);
         for (const void *p : {(const void *)b.store, (const void *)b.scale, (const void *)b.amax,
                               (const void *)b.rec, (const void *)b.shots, (const void *)b.mh, (const void *)b.mp,
@@ -874,8 +874,10 @@ template <typename T> struct Ctx : CtxBase {
         return FWI_OK;
     }
 
-    // Shots per group for a batch: groups need identical windows.  The tile
-    // passes are latency-bound, so many short blocks beat few long ones: the
+    // Shots per group of the interior tile passes (a group of several windows
+    // runs their MIXED kernels; the layer passes then take one shot per
+    // block).  The tile passes are latency-bound, so many short blocks beat
+    // few long ones: the
     // group count gives about three waves of adjoint tile blocks (3 resident
     // per SM of a 152-SM GB300).  Measured on 601 x 301, 32 shots: 5 shots
     // per group (7 groups) 56.8 shots/s, 8: 53.8, 3: 52.3, 16: 40.6.
@@ -889,8 +891,6 @@ template <typename T> struct Ctx : CtxBase {
     int shots_per_group(const std::vector<DevShot> &bs, int nxm) const
     {
         if (!use_tma) return 1;
-        for (const DevShot &d : bs)
-            if (d.x0 != bs[0].x0 || d.nx != bs[0].nx) return 1;
         if (const char *e = getenv("FWI_SHOTS_PER_GROUP")) {  // tuning override
             const int v = atoi(e);
             if (v >= 1) return std::min(v, 64);
@@ -959,7 +959,8 @@ template <typename T> struct Ctx : CtxBase {
         fwi::TileGrid tg;
         if (use_tma && uniform_windows(bs)) tg = fwi::tile_grid(nxm, nz, cfg.cpml);
         c.inline_strip = tg.inline_strip ? 1 : 0;
-        c.sg_layer = c.sg == 1 ? 1 : layer_shots_per_group((int)bs.size(), nxm, tg.xbase, tg.zbase);
+        c.sg_layer = c.sg == 1 || !uniform_windows(bs) ? 1
+                                                       : layer_shots_per_group((int)bs.size(), nxm, tg.xbase, tg.zbase);
         return c;
     }
 
@@ -982,13 +983,16 @@ template <typename T> struct Ctx : CtxBase {
         tuned.push_back({key, c});
     }
 
-    // Groups of more than one shot need one window for all (default_choice
-    // and the tuner keep to that).
+    // A batch of several windows: the interior passes' groups run the MIXED
+    // kernels, the layer passes take one shot per block, no in-tile memory
+    // variables (no tile origin fits every window's bands).
     void apply_choice(Batch<T> &b, const std::vector<DevShot> &bs, int nxm, const Choice &c) const
     {
+        const bool uniform = uniform_windows(bs);
         b.sg = c.sg;
-        b.sg_layer = c.sg_layer;
-        if (use_tma && uniform_windows(bs)) {  // one tile grid fits every shot
+        b.sg_layer = uniform ? c.sg_layer : 1;
+        b.mixed = use_tma && !uniform && c.sg > 1 ? 1 : 0;
+        if (use_tma && uniform) {  // one tile grid fits every shot
             const fwi::TileGrid tg = fwi::tile_grid(nxm, nz, cfg.cpml);
             b.xbase = tg.xbase;
             b.zbase = tg.zbase;
@@ -1138,6 +1142,7 @@ template <typename T> struct Ctx : CtxBase {
         b.sg_layer = 1;
         b.xbase = b.zbase = 0;
         b.inline_strip = 0;
+        b.mixed = 0;
         b.tma = use_tma ? (const void *)&maps : nullptr;
         return b;
     }
@@ -1595,9 +1600,11 @@ template <typename T> struct Ctx : CtxBase {
                     }
                     return FWI_OK;
                 };
-                if (!(tiles && uniform_windows(bs))) continue;  // groups of several shots need one window
+                if (!tiles) continue;
+                // several windows: only the interior groups vary (layer groups need one window)
+                const bool uniform = uniform_windows(bs);
                 const int cand[] = {1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 24, 32, 48, 64};
-                const fwi::TileGrid tg = fwi::tile_grid(nxm, nz, cfg.cpml);
+                const fwi::TileGrid tg = uniform ? fwi::tile_grid(nxm, nz, cfg.cpml) : fwi::TileGrid{};
                 for (int pass = 0; pass < 2; pass++) {
                     for (int v : cand)
                         if (v <= nb) {
@@ -1605,6 +1612,7 @@ template <typename T> struct Ctx : CtxBase {
                             c.sg = v;
                             if ((rc = consider(c))) return rc;
                         }
+                    if (!uniform) continue;
                     for (int v : cand)
                         if (v <= nb) {
                             Choice c = bp;
@@ -1664,10 +1672,13 @@ template <typename T> struct Ctx : CtxBase {
             int nxm = 0;
             for (const DevShot &d : bs) nxm = std::max(nxm, d.nx);
             Choices cb = c;
-            if (!(sizeof(T) == 4 && use_tma && uniform_windows(bs))) {
-                // several windows (or no tile passes): one shot per block
-                for (Choice *o : {&cb.fwd, &cb.adj}) {
+            if (!(sizeof(T) == 4 && use_tma)) {  // no tile passes: one shot per block
+                for (Choice *o : {&cb.fwd, &cb.adj})
                     if (o->sg != 1 || o->sg_layer != 1) return FWI_ERR_ARG;
+            }
+            if (!uniform_windows(bs)) {  // several windows: layer tiles take one shot per block
+                for (Choice *o : {&cb.fwd, &cb.adj}) {
+                    if (o->sg_layer != 1) return FWI_ERR_ARG;
                     o->inline_strip = 0;
                 }
             }

@@ -44,6 +44,8 @@ template <typename T> struct Batch {
     int sg_layer;           // the same for the FP32 layer tiles (their points are disjoint
                             // from the other passes', so the slots do not collide)
     int xbase, zbase;       // FP32 tile grid origin (TileGrid)
+    int mixed;              // FP32: the interior passes' groups hold several windows (their
+                            // MIXED kernels); the layer passes then take one shot per block
     int inline_strip;       // FP32: the layer tiles advance the CPML memory variables
     const void *tma;        // host copy of the batch's TMA tensor maps (FP32 path), or null
 };

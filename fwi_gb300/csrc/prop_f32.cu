@@ -30,8 +30,11 @@ inline dim3 tma_grid(const Batch<float> &b, int nx_max, int sg)
 template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
 {
     const size_t sm = fwd_tma_smem();
-    k_fwd_tma<ST><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, *static_cast<const TmaMaps *>(b.tma), g,
-                                                                       ntb, cur, slot, b.sg);
+    const TmaMaps &m = *static_cast<const TmaMaps *>(b.tma);
+    if (b.mixed)
+        k_fwd_tma<ST, true><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, g, ntb, cur, slot, b.sg);
+    else
+        k_fwd_tma<ST, false><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, g, ntb, cur, slot, b.sg);
 }
 
 template <int ST, bool EXACT, bool INLINE>
@@ -46,8 +49,13 @@ template <int ST, bool EXACT>
 void adj_interior(const Batch<float> &b, int nx_max, int j, int ntb, int cur, int zsel, int base, cudaStream_t st)
 {
     const size_t sm = adj_tma_smem();
-    k_adj_tma<ST, EXACT><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(
-        b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, base, b.sg);
+    const TmaMaps &m = *static_cast<const TmaMaps *>(b.tma);
+    if (b.mixed)
+        k_adj_tma<ST, EXACT, true><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, j, ntb, cur, zsel, base,
+                                                                                       b.sg);
+    else
+        k_adj_tma<ST, EXACT, false><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, j, ntb, cur, zsel, base,
+                                                                                        b.sg);
 }
 
 template <int ST, bool EXACT, bool INLINE>
@@ -134,13 +142,16 @@ template <int ST> cudaError_t allow_all()
 {
     cudaError_t e = cudaSuccess;
     auto keep = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
-    keep(allow_smem(k_fwd_tma<ST>, fwd_tma_smem()));
+    keep(allow_smem(k_fwd_tma<ST, false>, fwd_tma_smem()));
+    keep(allow_smem(k_fwd_tma<ST, true>, fwd_tma_smem()));
     keep(allow_smem(k_fwd_layer<ST, true, true>, fwd_layer_smem()));
     keep(allow_smem(k_fwd_layer<ST, true, false>, fwd_layer_smem()));
     keep(allow_smem(k_fwd_layer<ST, false, true>, fwd_layer_smem()));
     keep(allow_smem(k_fwd_layer<ST, false, false>, fwd_layer_smem()));
-    keep(allow_smem(k_adj_tma<ST, true>, adj_tma_smem()));
-    keep(allow_smem(k_adj_tma<ST, false>, adj_tma_smem()));
+    keep(allow_smem(k_adj_tma<ST, true, false>, adj_tma_smem()));
+    keep(allow_smem(k_adj_tma<ST, false, false>, adj_tma_smem()));
+    keep(allow_smem(k_adj_tma<ST, true, true>, adj_tma_smem()));
+    keep(allow_smem(k_adj_tma<ST, false, true>, adj_tma_smem()));
     keep(allow_smem(k_adj_layer<ST, true, true>, adj_layer_smem()));
     keep(allow_smem(k_adj_layer<ST, true, false>, adj_layer_smem()));
     keep(allow_smem(k_adj_layer<ST, false, true>, adj_layer_smem()));
@@ -200,13 +211,14 @@ template <>
 void launch_rebuild_step<float>(const Batch<float> &rb, int nx_max, int g, int ntb, int cur, const float *ring,
                                 long ring_len, int img_slot, cudaStream_t st)
 {
-    const dim3 grid = tma_grid(rb, nx_max, rb.sg);
+    const int sg = rb.mixed ? 1 : rb.sg;  // a group of the rebuild shares one window
+    const dim3 grid = tma_grid(rb, nx_max, sg);
     const size_t sm = rebuild_tma_smem();
     const TmaMaps &m = *static_cast<const TmaMaps *>(rb.tma);
     switch (rb.store_type) {
-    case kStoreHalf: k_rebuild_tma<kStoreHalf><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, rb.sg, img_slot); break;
-    case kStoreBf16: k_rebuild_tma<kStoreBf16><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, rb.sg, img_slot); break;
-    default: k_rebuild_tma<kStoreNative><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, rb.sg, img_slot); break;
+    case kStoreHalf: k_rebuild_tma<kStoreHalf><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, sg, img_slot); break;
+    case kStoreBf16: k_rebuild_tma<kStoreBf16><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, sg, img_slot); break;
+    default: k_rebuild_tma<kStoreNative><<<grid, kTmaThreads, sm, st>>>(rb, m, g, ntb, cur, ring, ring_len, sg, img_slot); break;
     }
 }
 

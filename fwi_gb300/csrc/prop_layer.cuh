@@ -103,7 +103,7 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
         q.so = (long)s * b.slot;
         q.rec_base = sh.rec_off + (long)it * (sh.rx1 - sh.rx0) - sh.rx0;
         q.img = ((long)s * b.n_img + (img_slot >= 0 ? img_slot : 0)) * 2 * b.slot;
-        q.sx = sh.sx; q.sz = sh.sz; q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.pad = 0;
+        q.sx = sh.sx; q.sz = sh.sz; q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.wx0 = sh.x0;
         q.w = b.wavelet[it];
         q.sc = 1.f;
         if (img_slot >= 0 && Cd::scaled) {
@@ -376,7 +376,7 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
         q.res_base = sh.rec_off + (long)(mm - 1) * (sh.rx1 - sh.rx0) - sh.rx0;
         const bool im = mm - 1 - lag >= 0;
         q.img = im ? ((long)s * b.n_img + (img_g - img_base)) * 2 * b.slot : -1;
-        q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.pad = 0;
+        q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.wx0 = sh.x0;
         q.inv_sc = (im && Cd::scaled) ? 1.f / b.scale[(long)s * b.nt_max + img_g] : 1.f;
         ps[tid] = q;
     }

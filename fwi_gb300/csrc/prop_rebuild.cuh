@@ -43,7 +43,7 @@ k_rebuild_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int n
         q.so = (long)s * b.slot;
         q.rec_base = it - 1 >= 0 ? ((long)s * b.nt_max + (g - 1)) * ring_len : -1;  // ring of step g - 1
         q.img = ((long)s * b.n_img + img_slot) * 2 * b.slot;
-        q.sx = sh.sx; q.sz = sh.sz; q.rz = 0; q.rx0 = 0; q.rx1 = 0; q.pad = 0;
+        q.sx = sh.sx; q.sz = sh.sz; q.rz = 0; q.rx0 = 0; q.rx1 = 0; q.wx0 = sh.x0;
         q.w = b.wavelet[it];
         q.sc = Cd::scaled ? image_scale(b.amax[(long)s * (b.nt_max + 1) + g], (float)b.inv_dh2) : 1.f;
         if (Cd::scaled && blockIdx.x == 0 && blockIdx.y == 0) b.scale[(long)s * b.nt_max + g] = q.sc;

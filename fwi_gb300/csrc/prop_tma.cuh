@@ -105,15 +105,21 @@ __device__ __forceinline__ bool stage_release(bool ok, uint64_t *bar, int a, int
     return false;
 }
 
-__device__ __forceinline__ int active_shots(const Batch<float> &b, int sg, int *act, bool adjoint, int step, int ntb)
+// The shots of this block's group that run at this step; with aw > 0 (a
+// group of several windows), only those for which the tile at (x0, z0) is an
+// interior tile (tile_role 1 for width aw) of their own window.
+__device__ __forceinline__ int active_shots(const Batch<float> &b, int sg, int *act, bool adjoint, int step, int ntb,
+                                            int x0 = 0, int z0 = 0, int aw = 0)
 {
     __shared__ int n_s;
     if (threadIdx.x == 0) {
         const int s0 = blockIdx.z * sg, s1 = min(s0 + sg, b.B);
         int n = 0;
         for (int s = s0; s < s1; s++) {
-            const int nt = b.shots[s].nt;
-            if (adjoint ? (step < nt) : (step - (ntb - nt) >= 0)) act[n++] = s;
+            const DevShot &d = b.shots[s];
+            if (!(adjoint ? (step < d.nt) : (step - (ntb - d.nt) >= 0))) continue;
+            if (aw > 0 && tile_role(x0, z0, d.nx, b.nz, aw) != 1) continue;
+            act[n++] = s;
         }
         n_s = n;
     }
@@ -189,12 +195,17 @@ struct FwdShot {
     long so;        // shot offset in the per-shot arrays
     long rec_base;  // record index of column 0 at this step (receivers at rec_base + ix)
     long img;       // image offset, in elements of the store type
-    int sx, sz, rz, rx0, rx1, pad;
+    int sx, sz, rz, rx0, rx1, wx0;  // source, receivers; wx0: model column of window column 0
     float w, sc;    // wavelet sample, image scale
 };
 
 // Interior tiles: no CPML term, so the images are the plain stencils in both modes.
-template <int ST>
+// MIXED: the group's shots have several windows (one tile grid, in window
+// coordinates, for all): the block keeps the shots for which its tile is an
+// interior tile of their own window and reads the models at each shot's own
+// columns; its interior mask depends on the row only (every column of an
+// interior tile is an interior column).
+template <int ST, bool MIXED>
 __global__ void __launch_bounds__(kTmaThreads, 4)
 k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, int cur, int img_slot, int sg)
 {
@@ -206,10 +217,10 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     __shared__ FwdShot ps[kMaxGroup];
     const int tid = threadIdx.x;
     const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
-    const DevShot gsh = b.shots[blockIdx.z * sg];  // every shot of the group has this window
+    const DevShot gsh = b.shots[blockIdx.z * sg];  // unless MIXED, every shot of the group has this window
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
-    if (tile_role(x0, z0, nx, nz, cpml) != 1) return;
-    const int na = active_shots(b, sg, act, false, g, ntb);
+    if (!MIXED && tile_role(x0, z0, nx, nz, cpml) != 1) return;
+    const int na = MIXED ? active_shots(b, sg, act, false, g, ntb, x0, z0, cpml) : active_shots(b, sg, act, false, g, ntb);
     if (na == 0) return;
     if (tid == 0) {
         for (int k = 0; k < kStages; k++) mbar_init(&bar[k], 1);
@@ -223,7 +234,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
         q.so = (long)s * b.slot;
         q.rec_base = sh.rec_off + (long)it * (sh.rx1 - sh.rx0) - sh.rx0;
         q.img = ((long)s * b.n_img + (img_slot >= 0 ? img_slot : 0)) * 2 * b.slot;
-        q.sx = sh.sx; q.sz = sh.sz; q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.pad = 0;
+        q.sx = sh.sx; q.sz = sh.sz; q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.wx0 = sh.x0;
         q.w = b.wavelet[it];
         q.sc = 1.f;
         if (img_slot >= 0 && Cd::scaled) {
@@ -251,13 +262,13 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int ix = ix0 + q;
-        m[q] = ix < nx && iz < nz && interior(ix, iz, nx, nz);
+        m[q] = MIXED ? (iz > 3 && iz < nz - 4) : (ix < nx && iz < nz && interior(ix, iz, nx, nz));
         any |= m[q];
         all &= m[q];
         const long mi = (long)iz * b.mpitch + gsh.x0 + ix;
-        mh[q] = m[q] ? b.mh[mi] : 0.f;
-        mp[q] = m[q] ? b.mp[mi] : 0.f;
-        mn[q] = m[q] ? b.mn[mi] : 0.f;
+        mh[q] = !MIXED && m[q] ? b.mh[mi] : 0.f;
+        mp[q] = !MIXED && m[q] ? b.mp[mi] : 0.f;
+        mn[q] = !MIXED && m[q] ? b.mn[mi] : 0.f;
     }
     const long ipt = (long)iz * pitch + ix0;
     float *const Pn0 = b.lvl[1 - cur], *const Fn0 = b.lvl[3 - cur];
@@ -269,6 +280,15 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
         if (any) {  // own points only: issued before the wait, in flight during it
             vP = ld4(Pv0 + so + ipt);
             vF = ld4(Fv0 + so + ipt);
+            if (MIXED) {  // this shot's model columns
+                const long mi = (long)iz * b.mpitch + sh.wx0 + ix0;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    mh[q] = m[q] ? b.mh[mi + q] : 0.f;
+                    mp[q] = m[q] ? b.mp[mi + q] : 0.f;
+                    mn[q] = m[q] ? b.mn[mi + q] : 0.f;
+                }
+            }
         }
         const bool ok = mbar_wait(&bar[a % kStages], (a / kStages) & 1);
         const FwdStage &S = stage[a % kStages];
@@ -371,11 +391,15 @@ struct AdjShot {
     long so;        // shot offset in the per-shot arrays
     long res_base;  // residual index of column 0 at this step (residual at res_base + ix)
     long img;       // image offset in elements of the store type, < 0: no image this step
-    int rz, rx0, rx1, pad;  // receiver row and columns
+    int rz, rx0, rx1, wx0;  // receiver row and columns; model column of window column 0
+    int nx;         // window width
     float inv_sc;   // inverse image scale
 };
 
-template <int ST, bool EXACT>
+// MIXED (several windows in the group, see k_fwd_tma): the model tiles are
+// staged per shot, at the shot's own columns, and each shot's imaging goes
+// to its own gradient slot (shot s: slot s) instead of a sum per group.
+template <int ST, bool EXACT, bool MIXED>
 __global__ void __launch_bounds__(kTmaThreads, 4)
 k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int zsel, int img_base,
           int sg)
@@ -400,8 +424,8 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     const DevShot gsh = b.shots[grp * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
     const int aw = EXACT ? cpml + kRad : cpml;
-    if (tile_role(x0, z0, nx, nz, aw) != 1) return;
-    const int na = active_shots(b, sg, act, true, j, ntb);
+    if (!MIXED && tile_role(x0, z0, nx, nz, aw) != 1) return;
+    const int na = MIXED ? active_shots(b, sg, act, true, j, ntb, x0, z0, aw) : active_shots(b, sg, act, true, j, ntb);
     if (na == 0) return;
     const int lag = EXACT ? 0 : 1;
     const int img_g = ntb - 1 - lag - j;  // global step of the image this iteration needs
@@ -418,7 +442,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
         q.res_base = sh.rec_off + (long)(mm - 1) * (sh.rx1 - sh.rx0) - sh.rx0;
         const bool im = mm - 1 - lag >= 0;
         q.img = im ? ((long)s * b.n_img + (img_g - img_base)) * 2 * b.slot : -1;
-        q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.pad = 0;
+        q.rz = sh.rz; q.rx0 = sh.rx0; q.rx1 = sh.rx1; q.wx0 = sh.x0; q.nx = sh.nx;
         q.inv_sc = (im && Cd::scaled) ? 1.f / b.scale[(long)s * b.nt_max + img_g] : 1.f;
         ps[tid] = q;
     }
@@ -433,22 +457,28 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     };
     if (tid == 0)
         for (int k = 0; k < min(kAdjStages, na); k++) issue(k);
-    // model tiles of the group's window: v_hor, v_nmo with the x-halo, v_po with the z-halo
-    for (int k = tid; k < TT * TH; k += kTmaThreads) {
-        const int rr = k / TH, cc = k - rr * TH;
-        const int gx = x0 - kRad + cc, gz = z0 + rr;
-        const bool in = gx >= 0 && gx < nx && gz >= 0 && gz < nz;
-        const long mi = (long)gz * b.mpitch + gsh.x0 + gx;
-        MH[rr][cc] = in ? b.mh[mi] : 0.f;
-        MN[rr][cc] = in ? b.mn[mi] : 0.f;
+    // model tiles of a window (its first model column wx0, width wnx): v_hor, v_nmo with
+    // the x-halo, v_po with the z-halo
+    auto stage_models = [&](int wx0, int wnx) {
+        for (int k = tid; k < TT * TH; k += kTmaThreads) {
+            const int rr = k / TH, cc = k - rr * TH;
+            const int gx = x0 - kRad + cc, gz = z0 + rr;
+            const bool in = gx >= 0 && gx < wnx && gz >= 0 && gz < nz;
+            const long mi = (long)gz * b.mpitch + wx0 + gx;
+            MH[rr][cc] = in ? b.mh[mi] : 0.f;
+            MN[rr][cc] = in ? b.mn[mi] : 0.f;
+        }
+        for (int k = tid; k < TH * TT; k += kTmaThreads) {
+            const int rr = k / TT, cc = k - rr * TT;
+            const int gx = x0 + cc, gz = z0 - kRad + rr;
+            const bool in = gx < wnx && gz >= 0 && gz < nz;
+            MP[rr][cc] = in ? b.mp[(long)gz * b.mpitch + wx0 + gx] : 0.f;
+        }
+    };
+    if (!MIXED) {
+        stage_models(gsh.x0, nx);
+        __syncthreads();  // the model tiles, before any thread's first U, V (no block barrier before that)
     }
-    for (int k = tid; k < TH * TT; k += kTmaThreads) {
-        const int rr = k / TT, cc = k - rr * TT;
-        const int gx = x0 + cc, gz = z0 - kRad + rr;
-        const bool in = gx < nx && gz >= 0 && gz < nz;
-        MP[rr][cc] = in ? b.mp[(long)gz * b.mpitch + gsh.x0 + gx] : 0.f;
-    }
-    __syncthreads();  // the model tiles, before any thread's first U, V (no block barrier before that)
     const int c4 = 4 * (tid & 7), r = tid >> 3;
     const int ix0 = x0 + c4, iz = z0 + r;
     bool m[4];  // interior points
@@ -456,7 +486,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int ix = ix0 + q;
-        m[q] = ix < nx && iz < nz && interior(ix, iz, nx, nz);
+        m[q] = MIXED ? (iz > 3 && iz < nz - 4) : (ix < nx && iz < nz && interior(ix, iz, nx, nz));
         any |= m[q];
         all &= m[q];
     }
@@ -478,7 +508,10 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                 Vec4Store<SI>::get(img + b.slot + ipt, iH);
             }
         }
+        // MIXED: this shot's model tiles (the previous shot's U, V are done: stage_release)
+        if (MIXED) stage_models(ps[a].wx0, ps[a].nx);
         const bool ok = mbar_wait(&bar[a % kAdjStages], (a / kAdjStages) & 1);
+        if (MIXED) __syncthreads();  // the model tiles, before U, V
         const Stage &S = stage[a % kAdjStages];
         // U = dt^2 (v_hor lP + v_nmo lF) on the x-halo tile, V = dt^2 v_po (lP + lF) on the z-halo tile
         // (from whatever the stage holds if this thread's wait gave up: the iteration is then discarded)
@@ -559,6 +592,29 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                     ap[q] += kk * Hv * (nP[q] + nF[q]);
                     an[q] += kk * Gv * nF[q];
                 }
+                if (MIXED) {
+                    // this shot's slot: g[act[a]] += its imaging, as reductions that the
+                    // thread does not wait for.  One add per point and launch (each slot
+                    // point belongs to one block and thread), so the sum is the plain
+                    // read-modify-write's, bit for bit.
+                    const long gi = (long)act[a] * b.slot + ipt;
+                    float *g0 = b.g[0] + gi, *g1 = b.g[1] + gi, *g2 = b.g[2] + gi;
+                    if (all) {
+                        atomicAdd(reinterpret_cast<float4 *>(g0), make_float4(ah[0], ah[1], ah[2], ah[3]));
+                        atomicAdd(reinterpret_cast<float4 *>(g1), make_float4(ap[0], ap[1], ap[2], ap[3]));
+                        atomicAdd(reinterpret_cast<float4 *>(g2), make_float4(an[0], an[1], an[2], an[3]));
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (m[q]) {
+                                atomicAdd(g0 + q, ah[q]);
+                                atomicAdd(g1 + q, ap[q]);
+                                atomicAdd(g2 + q, an[q]);
+                            }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q++) ah[q] = ap[q] = an[q] = 0.f;
+                }
             }
         }
         if (!stage_release(!bad, bar, a, na, kAdjStages, b.status)) return;  // stage, U and V are free again
@@ -567,7 +623,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
             issue(a + kAdjStages);
         }
     }
-    if (!any) return;
+    if (MIXED || !any) return;
     // one read-modify-write per group: g[grp] += the group's imaging
     const long gi = (long)grp * b.slot + ipt;
     float *g0 = b.g[0] + gi, *g1 = b.g[1] + gi, *g2 = b.g[2] + gi;

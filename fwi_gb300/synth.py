@@ -194,7 +194,7 @@ def c4(seed=4, shots=256):
         sx = x0 + ap // 2
         sh.append(dict(sx=sx, sz=2 + FRAME, rz=2 + FRAME, rx0=x0 + FRAME, rx1=x0 + ap - FRAME, nt=nt, x0=x0, nxw=ap))
     mask = np.concatenate([(rng.random(s["rx1"] - s["rx0"]) >= 0.10).astype(np.uint8) for s in sh])
-    w = Workload("C4 uneven batch 4001x1201 256 shots", nx, nzp + 8, 10.0, 8e-4, max(s["nt"] for s in sh), 12.0,
+    w = Workload(f"C4 uneven batch 4001x1201 {shots} shots", nx, nzp + 8, 10.0, 8e-4, max(s["nt"] for s in sh), 12.0,
                  20, sh, _pad(vel), _pad(eps), _pad(dl), mask=mask)
     w.vel0, w.eps0, w.delta0 = (_gauss_smooth(a, 10) for a in (w.vel, w.eps, w.delta))
     return w

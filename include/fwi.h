@@ -244,8 +244,9 @@ long fwi_last_launches(void *ctx);
 /* Autotuner (no counterpart in the reference).  The FP32 tile passes have a
  * fixed 32 x 32 point tile (the TMA box and four points per thread); what
  * shapes their work is how many shots one block takes through the tile (the
- * interior and the layer tile passes separately; more than one needs every
- * shot of the batch on one window) and whether the layer tiles advance the
+ * interior and the layer tile passes separately; a layer block takes more
+ * than one only when every shot of the batch has one window, an interior
+ * block also from several windows) and whether the layer tiles advance the
  * CPML memory variables themselves or after a strip pass; the forward and
  * the adjoint are chosen separately.  fwi_autotune times `steps` steps of
  * candidate choices of each phase for each batch the shots form (coordinate
@@ -273,7 +274,7 @@ int fwi_autotune(void *ctx, const fwi_shot *shots, int nshots, int steps, fwi_tu
 /* Records t's choice (forward, adjoint) for the batch shapes the shots form,
  * as fwi_autotune does: a choice tuned once, kept and given again gives the
  * same results bit for bit.  FWI_ERR_ARG when it does not fit: a group size
- * outside 1..64, or above 1 for a batch of several windows. */
+ * outside 1..64, or a layer group above 1 for a batch of several windows. */
 int fwi_set_tuning(void *ctx, const fwi_shot *shots, int nshots, const fwi_tuning *t);
 
 /* CUDA graphs (no counterpart in the reference, which launches every kernel

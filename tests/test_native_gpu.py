@@ -429,3 +429,33 @@ def test_edge_geometries_match_fp64_oracle(case):
     assert abs(Jg - J) <= 1e-5 * J
     for a, b in zip(gg, g):
         assert rel_l2(a, b) <= 1e-4, rel_l2(a, b)
+
+
+@pytest.mark.parametrize("store", ["full", "checkpoint", "boundary"])
+def test_groups_of_several_windows_are_bitwise_one_shot_per_block(exact_case, store):
+    """The interior passes' groups of several windows (MIXED kernels: per-shot
+    tile roles, model columns and gradient slots) give the results of one
+    shot per block bit for bit, and the FP64 oracle's within 1e-4."""
+    from fwi_gb300 import (Context, MODE_EXACT, PREC_FP32, STORE_BOUNDARY, STORE_CHECKPOINT, STORE_FULL,
+                           make_shots)
+    p, shots, obs, mask, J, g = exact_case
+    st = dict(full=STORE_FULL, checkpoint=STORE_CHECKPOINT, boundary=STORE_BOUNDARY)[store]
+    sh = make_shots(shots)
+    res = []
+    for sg in (1, 2):
+        ctx = Context(nx=p["nx"], nz=p["nz"], dh=p["dh"], dt=p["dt"], cpml=p["cpml"], f_cpml=p["f"],
+                      nt_max=p["nt"], max_shots=2, mode=MODE_EXACT, precision=PREC_FP32, store=st,
+                      ckpt_every=37 if store == "checkpoint" else 0)
+        ctx.set_wavelet(wavelet(p).astype(np.float32))
+        ctx.set_model(*(np.ascontiguousarray(p[k], np.float32) for k in ("vh", "vp", "vn")))
+        c = dict(shots_per_group=sg, layer_shots_per_group=1, inline_strip=0)
+        ctx.set_tuning(sh, dict(forward=c, adjoint=c))
+        res.append(ctx.gradient(sh, obs.astype(np.float32), mask))
+        del ctx
+    assert res[0][0] == res[1][0]
+    for a, b in zip(res[0][1:], res[1][1:]):
+        assert np.array_equal(a, b)
+    if store == "full":
+        assert abs(res[1][0] - J) <= 1e-5 * J
+        for a, b in zip(res[1][1:], g):
+            assert rel_l2(a, b) <= 1e-4
