@@ -112,10 +112,11 @@ inline TileGrid tile_grid(int nx, int nz, int cpml)
 // 1 interior tile (no layer point), 2 layer tile.
 __host__ __device__ inline int tile_role(int x0, int z0, int nx, int nz, int aw)
 {
-    if (x0 > nx - 5 || z0 > nz - 5) return 0;
-    const int xa = x0 > 4 ? x0 : 4;
+    // the tile's interior points: columns [xa, xb], rows [za, zb]
+    const int xa = x0 > 4 ? x0 : 4, za = z0 > 4 ? z0 : 4;
     const int xb = x0 + kTileEdge - 1 < nx - 5 ? x0 + kTileEdge - 1 : nx - 5;
     const int zb = z0 + kTileEdge - 1 < nz - 5 ? z0 + kTileEdge - 1 : nz - 5;
+    if (xa > xb || za > zb) return 0;  // the frame only (or beyond the window)
     return (xa < aw || xb > nx - aw - 1 || zb > nz - aw - 1) ? 2 : 1;
 }
 
