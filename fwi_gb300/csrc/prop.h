@@ -120,6 +120,57 @@ __host__ __device__ inline int tile_role(int x0, int z0, int nx, int nz, int aw)
     return (xa < aw || xb > nx - aw - 1 || zb > nz - aw - 1) ? 2 : 1;
 }
 
+// Boundary storage (FWI_STORE_BOUNDARY, prop_boundary.cuh): the ring the
+// forward saves around the CPML-free region of each window.
+// Ring of an nx x nz window: P at columns [cpml-4, cpml) and [nx-cpml,
+// nx-cpml+4) of rows [4, nz-cpml); F at rows [nz-cpml, nz-cpml+4) of
+// columns [cpml, nx-cpml).  Enumerated P-left, P-right, then F-bottom, x fastest.
+struct Ring {
+    int nx, nz, cpml, h, w;  // h rows of R, w columns of R
+    __host__ __device__ static Ring make(int nx, int nz, int cpml)
+    {
+        Ring r;
+        r.nx = nx; r.nz = nz; r.cpml = cpml;
+        r.h = nz - cpml - 4;
+        r.w = nx - 2 * cpml;
+        if (r.h < 0) r.h = 0;
+        if (r.w < 0) r.w = 0;
+        return r;
+    }
+    __host__ __device__ long count() const { return 8L * h + 4L * w; }
+    // The inverse of point(): the ring index of (ix, iz) and whether it is an
+    // F point, or -1 for a point off the ring.
+    __host__ __device__ long index(int ix, int iz, bool &isF) const
+    {
+        isF = false;
+        if (iz >= 4 && iz < nz - cpml) {
+            if (ix >= cpml - 4 && ix < cpml) return (long)(iz - 4) * 4 + (ix - (cpml - 4));
+            if (ix >= nx - cpml && ix < nx - cpml + 4) return 4L * h + (long)(iz - 4) * 4 + (ix - (nx - cpml));
+            return -1;
+        }
+        if (iz >= nz - cpml && iz < nz - cpml + 4 && ix >= cpml && ix < nx - cpml) {
+            isF = true;
+            return 8L * h + (long)(iz - (nz - cpml)) * w + (ix - cpml);
+        }
+        return -1;
+    }
+    // point k: (ix, iz) and whether it belongs to F (else P)
+    __host__ __device__ void point(long k, int &ix, int &iz, bool &isF) const
+    {
+        if (k < 8L * h) {
+            const int side = (int)(k / (4L * h)), kk = (int)(k - side * 4L * h);
+            iz = 4 + kk / 4;
+            ix = (side == 0 ? cpml - 4 : nx - cpml) + kk % 4;
+            isF = false;
+            return;
+        }
+        k -= 8L * h;
+        iz = nz - cpml + (int)(k / w);
+        ix = cpml + (int)(k % w);
+        isF = true;
+    }
+};
+
 // Streams of a step.  The FP32 path runs the interior tiles on `main` and
 // the strip pass (CPML memory variables) followed by the layer tiles on
 // `side`, both from the current time level, and `main` joins `side` before

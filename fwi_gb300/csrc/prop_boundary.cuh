@@ -24,39 +24,6 @@
 
 namespace fwi {
 
-// Ring of an nx x nz window: P at columns [cpml-4, cpml) and [nx-cpml,
-// nx-cpml+4) of rows [4, nz-cpml); F at rows [nz-cpml, nz-cpml+4) of
-// columns [cpml, nx-cpml).  Enumerated P-left, P-right, then F-bottom, x fastest.
-struct Ring {
-    int nx, nz, cpml, h, w;  // h rows of R, w columns of R
-    __host__ __device__ static Ring make(int nx, int nz, int cpml)
-    {
-        Ring r;
-        r.nx = nx; r.nz = nz; r.cpml = cpml;
-        r.h = nz - cpml - 4;
-        r.w = nx - 2 * cpml;
-        if (r.h < 0) r.h = 0;
-        if (r.w < 0) r.w = 0;
-        return r;
-    }
-    __host__ __device__ long count() const { return 8L * h + 4L * w; }
-    // point k: (ix, iz) and whether it belongs to F (else P)
-    __host__ __device__ void point(long k, int &ix, int &iz, bool &isF) const
-    {
-        if (k < 8L * h) {
-            const int side = (int)(k / (4L * h)), kk = (int)(k - side * 4L * h);
-            iz = 4 + kk / 4;
-            ix = (side == 0 ? cpml - 4 : nx - cpml) + kk % 4;
-            isF = false;
-            return;
-        }
-        k -= 8L * h;
-        iz = nz - cpml + (int)(k / w);
-        ix = cpml + (int)(k % w);
-        isF = true;
-    }
-};
-
 // ring[s][g][k] <- the state P^g, F^g of the ring points, for the shots active at
 // global step g (called before step g).
 template <typename T>

@@ -73,15 +73,7 @@ k_rebuild_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int n
         inR[q] = in_rebuild_region(ix, iz, nx, nz, cpml);
         any |= inR[q];
         all &= inR[q];
-        rk[q] = -1;
-        rF[q] = false;
-        if (iz >= 4 && iz < nz - cpml) {
-            if (ix >= cpml - 4 && ix < cpml) rk[q] = (long)(iz - 4) * 4 + (ix - (cpml - 4));
-            else if (ix >= nx - cpml && ix < nx - cpml + 4) rk[q] = 4L * R.h + (long)(iz - 4) * 4 + (ix - (nx - cpml));
-        } else if (iz >= nz - cpml && iz < nz - cpml + 4 && ix >= cpml && ix < nx - cpml) {
-            rk[q] = 8L * R.h + (long)(iz - (nz - cpml)) * R.w + (ix - cpml);
-            rF[q] = true;
-        }
+        rk[q] = R.index(ix, iz, rF[q]);
         anyRing |= rk[q] >= 0;
         const long mi = (long)iz * b.mpitch + gsh.x0 + ix;
         mh[q] = inR[q] ? b.mh[mi] : 0.f;

@@ -12,6 +12,7 @@
 //     groups of several windows: every column of the tile is an interior
 //     column (its mask depends on the row only), and the tile with its 4-point
 //     halo lies inside the window (columns) and above the last row.
+//  4. The boundary ring's index of a point inverts its enumeration.
 #include "common.cuh"
 #include "prop.h"
 
@@ -66,6 +67,41 @@ static int check(int nx, int nz, int cpml)
     return 0;
 }
 
+// The boundary ring (FWI_STORE_BOUNDARY): index() inverts point() over the
+// whole ring and gives -1 for every other point of the window.
+static int check_ring(int nx, int nz, int cpml)
+{
+    const Ring R = Ring::make(nx, nz, cpml);
+    for (long k = 0; k < R.count(); k++) {
+        int ix, iz;
+        bool f, f2;
+        R.point(k, ix, iz, f);
+        if (R.index(ix, iz, f2) != k || f2 != f) {
+            printf("FAIL ring nx=%d nz=%d cpml=%d k=%ld\n", nx, nz, cpml, k);
+            return 1;
+        }
+    }
+    long n = 0;
+    for (int iz = 0; iz < nz; iz++)
+        for (int ix = 0; ix < nx; ix++) {
+            bool f;
+            const bool onP = iz >= 4 && iz < nz - cpml &&
+                             ((ix >= cpml - 4 && ix < cpml) || (ix >= nx - cpml && ix < nx - cpml + 4));
+            const bool onF = iz >= nz - cpml && iz < nz - cpml + 4 && ix >= cpml && ix < nx - cpml;
+            const long k = R.index(ix, iz, f);
+            if ((k >= 0) != (onP || onF) || (k >= 0 && f != onF)) {
+                printf("FAIL ring point nx=%d nz=%d cpml=%d (%d, %d)\n", nx, nz, cpml, ix, iz);
+                return 1;
+            }
+            n += k >= 0;
+        }
+    if (n != R.count()) {
+        printf("FAIL ring count nx=%d nz=%d cpml=%d\n", nx, nz, cpml);
+        return 1;
+    }
+    return 0;
+}
+
 int main()
 {
     long cases = 0;
@@ -86,6 +122,12 @@ int main()
         if (check(nx, 1209, 20)) return 1;
         cases++;
     }
+    for (int cpml : {8, 12, 20})
+        for (int nx : {2 * cpml + 9, 72, 137, 609})
+            for (int nz : {cpml + 9, 56, 309}) {
+                if (check_ring(nx, nz, cpml)) return 1;
+                cases++;
+            }
     printf("OK %ld\n", cases);
     return 0;
 }

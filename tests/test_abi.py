@@ -73,6 +73,14 @@ def test_config_defaults_and_bytes(built):
     cfg.store_prec = native.SPREC_FP16
     b4h = built.fwi_config_bytes(C.byref(cfg))
     assert b1 < b4 and b4h < b4
+    # long records: checkpoints and boundary rings need far less than every step's images
+    cfg.nt_max = 6000
+    full = built.fwi_config_bytes(C.byref(cfg))
+    cfg.store = native.STORE_CHECKPOINT
+    ckpt = built.fwi_config_bytes(C.byref(cfg))
+    cfg.store = native.STORE_BOUNDARY
+    ring = built.fwi_config_bytes(C.byref(cfg))
+    assert ckpt < full / 4 and ring < full / 4
 
 
 def test_invalid_configuration_is_rejected_before_any_device_call(built):
