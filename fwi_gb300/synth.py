@@ -210,7 +210,7 @@ def c5(seed=5, shots=512, nt=8000):
     vel = np.where(wedge, 4500.0, vel)
     eps = np.full((nzp, nxp), 0.12)
     dl = np.full((nzp, nxp), 0.06)
-    w = Workload("C5 multiscale 4001x1201 nt=8000 512 shots", nxp + 8, nzp + 8, 10.0, 8e-4, nt, 3.0, 20,
+    w = Workload(f"C5 multiscale 4001x1201 nt={nt} {shots} shots", nxp + 8, nzp + 8, 10.0, 8e-4, nt, 3.0, 20,
                  _surface_shots(nxp, shots, nt), _pad(vel), _pad(eps), _pad(dl), bands=[3.0, 6.0, 9.0, 12.0])
     w.vel0, w.eps0, w.delta0 = (_gauss_smooth(a, 10) for a in (w.vel, w.eps, w.delta))
     return w
