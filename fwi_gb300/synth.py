@@ -70,6 +70,11 @@ class Workload:
         vmax = float((self.vel * np.sqrt(1 + 2 * np.maximum(self.eps, self.delta))).max())
         return vmax * self.dt / self.dh
 
+    def __post_init__(self):
+        # the true model's fastest speed bounds the smoothed initial model's
+        if self.cfl() > CFL_LIMIT:
+            raise ValueError(f"{self.name}: vmax dt / dh = {self.cfl():.4f} above the stability limit {CFL_LIMIT}")
+
 
 def _gauss_smooth(a, sigma):
     from scipy.ndimage import gaussian_filter
