@@ -16,6 +16,7 @@
 #include "tma.cuh"
 
 #include <cuda_fp16.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -442,6 +443,30 @@ inline unsigned elt_grid(long n)
     return (unsigned)std::max(1L, std::min(b, 152L * 8));
 }
 
+// Check of the bounded pipeline wait (fwi_check_bounded_wait): one block
+// waits, as the tile passes do, on an mbarrier phase that nothing completes
+// (no thread arrives, no copy is in flight), gives up after `polls` polls and
+// records kStatusTimeout in the status word, then returns.
+__global__ void k_check_bounded_wait(unsigned *status, long polls)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        fwi::mbar_init(&bar, 1);
+        fwi::mbar_init_fence();
+    }
+    __syncthreads();
+    const bool ok = fwi::mbar_wait(&bar, 0, polls);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(status, fwi::kStatusTimeout);
+}
+
+// Host range on the profiler timelines (NVTX; nothing without a tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // ------------------------------------------------------------------ the context
 
 struct CtxBase {
@@ -501,6 +526,7 @@ struct CtxBase {
                     double *, void *traces, bool grad) = 0;
     virtual int autotune(const fwi_shot *, int, int, fwi_tuning *) = 0;
     virtual int set_tuning(const fwi_shot *, int, const fwi_tuning *) = 0;
+    virtual int check_bounded_wait(long polls) = 0;
     virtual int first_step(float, float, float) = 0;
     virtual int lbfgs_direction(int, double *) = 0;
     virtual int lbfgs_update(float, float, float, int, int) = 0;
@@ -1262,6 +1288,7 @@ template <typename T> struct Ctx : CtxBase {
                 }
                 return k;
             };
+            NvtxRange fwd_range("fwi forward steps");
             rc = run_section(section_key(0), 0, nsamp, spts[0], [&]() -> int {
                 int cur = 0;
                 for (int g = 0; g < ntb; g++) {
@@ -1302,6 +1329,7 @@ template <typename T> struct Ctx : CtxBase {
             if (traces)
                 TRY(cudaMemcpyAsync((T *)traces + off[b0], rec, nrec_elems * sizeof(T), cudaMemcpyDefault, st));
             if (want_grad) {
+                NvtxRange adj_range("fwi adjoint steps + imaging");
                 rc = run_section(section_key(1), 1, nsamp, spts[1], [&]() -> int {
                     for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
                     for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
@@ -1488,6 +1516,7 @@ template <typename T> struct Ctx : CtxBase {
     // those before use, so results only depend on the choice recorded.
     int autotune(const fwi_shot *sh, int n, int steps, fwi_tuning *out) override
     {
+        NvtxRange range("fwi autotune");
         if (!have_model || !have_wavelet) return FWI_ERR_STATE;
         if (!sh || n <= 0 || steps <= 0) return FWI_ERR_ARG;
         std::vector<DevShot> all(n);
@@ -1647,6 +1676,21 @@ template <typename T> struct Ctx : CtxBase {
         return FWI_OK;
     }
 
+    // fwi_check_bounded_wait: the wait gives up, the status word says so, the
+    // context stays usable (the status word is cleared by every later call).
+    int check_bounded_wait(long polls) override
+    {
+        if (polls < 1 || polls > fwi::kWaitLimit) return FWI_ERR_ARG;
+        TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+        k_check_bounded_wait<<<1, 128, 0, st>>>(status, polls);
+        TRY_LAUNCH();
+        unsigned stat = 0;
+        TRY(cudaMemcpyAsync(&stat, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        TRY(cudaStreamSynchronize(st));
+        TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+        return (stat & fwi::kStatusTimeout) ? FWI_ERR_CUDA : FWI_OK;
+    }
+
     // Records choice t for the batch shapes the shots form.
     int set_tuning(const fwi_shot *sh, int n, const fwi_tuning *t) override
     {
@@ -1735,6 +1779,7 @@ template <typename T> struct Ctx : CtxBase {
 
     int lbfgs_direction(int m, double *stats) override
     {
+        NvtxRange range("fwi L-BFGS direction");
         if (m < 1 || m > kMaxHist) return FWI_ERR_ARG;
         if (!have_grad || !have_back) return FWI_ERR_STATE;
         int rc = ensure_history(m);
@@ -2068,6 +2113,12 @@ int fwi_set_tuning(void *ctx, const fwi_shot *shots, int nshots, const fwi_tunin
 {
     if (!ctx) return FWI_ERR_ARG;
     return as_ctx(ctx)->set_tuning(shots, nshots, t);
+}
+
+int fwi_check_bounded_wait(void *ctx, long polls)
+{
+    if (!ctx) return FWI_ERR_ARG;
+    return as_ctx(ctx)->check_bounded_wait(polls);
 }
 
 int fwi_set_graphs(void *ctx, int on)

@@ -37,11 +37,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
                  : "memory");
 }
 
-// Returns false if the phase did not complete within kWaitLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+// Returns false if the phase did not complete within `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, long limit = kWaitLimit)
 {
     const uint32_t a = smem_addr(bar);
-    for (long k = 0; k < kWaitLimit; k++) {
+    for (long k = 0; k < limit; k++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"

@@ -126,6 +126,7 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_last_launches", [_p], _l)
         _sig(L, "fwi_autotune", [_p, shotp, _i, _i, C.POINTER(Tuning)])
         _sig(L, "fwi_set_tuning", [_p, shotp, _i, C.POINTER(Tuning)])
+        _sig(L, "fwi_check_bounded_wait", [_p, _l])
         _sig(L, "fwi_set_graphs", [_p, _i])
         _sig(L, "fwi_graph_stats", [_p, _p])
         _sig(L, "fwi_strip_points", [_i, _i, _i, _p, _p, _l], _l)
@@ -436,6 +437,10 @@ class Context:
             for f, _ in PhaseChoice._fields_:
                 setattr(getattr(t, ph), f, int(choice[ph][f]))
         _check(lib().fwi_set_tuning(self._h, shots, len(shots), C.byref(t)), "fwi_set_tuning")
+
+    def check_bounded_wait(self, polls=64):
+        """Status of fwi_check_bounded_wait (FWI_ERR_CUDA: the wait gave up and said so)."""
+        return int(lib().fwi_check_bounded_wait(self._h, int(polls)))
 
     def set_graphs(self, on=True):
         """CUDA graph replay of repeated batch sections (on by default)."""

@@ -277,6 +277,15 @@ int fwi_autotune(void *ctx, const fwi_shot *shots, int nshots, int steps, fwi_tu
  * outside 1..64, or a layer group above 1 for a batch of several windows. */
 int fwi_set_tuning(void *ctx, const fwi_shot *shots, int nshots, const fwi_tuning *t);
 
+/* Check of the device-side failure path (no counterpart in the reference):
+ * one block waits, as the tile passes wait for their staged tiles, on a
+ * barrier phase that nothing completes, gives up after `polls` polls
+ * (1 .. 4194304, the tile passes' own limit) and records the timeout in the
+ * context's status word.  Returns FWI_ERR_CUDA when the timeout was seen,
+ * as a gradient call would after a wait that gave up; the context stays
+ * usable.  No fault, trap or unbounded wait is involved. */
+int fwi_check_bounded_wait(void *ctx, long polls);
+
 /* CUDA graphs (no counterpart in the reference, which launches every kernel
  * from the host).  A batch of fwi_gradient / fwi_misfit / fwi_forward runs as
  * two sections: the forward steps, and the adjoint with its image rebuild and

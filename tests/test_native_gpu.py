@@ -459,3 +459,19 @@ def test_groups_of_several_windows_are_bitwise_one_shot_per_block(exact_case, st
         assert abs(res[1][0] - J) <= 1e-5 * J
         for a, b in zip(res[1][1:], g):
             assert rel_l2(a, b) <= 1e-4
+
+
+def test_a_wait_that_gives_up_is_reported_and_the_context_stays_usable(exact_case):
+    """Failure detection on the device without a fault: a barrier wait that
+    nothing completes gives up after a few polls, the host gets FWI_ERR_CUDA
+    from the status word, and the context then computes the gradient a fresh
+    context computes, bit for bit."""
+    from fwi_gb300 import PREC_FP32, make_shots
+    p, shots, obs, mask, _, _ = exact_case
+    ctx, first = run_exact(p, shots, obs, mask, PREC_FP32)
+    assert ctx.check_bounded_wait(64) == -2  # FWI_ERR_CUDA
+    assert ctx.check_bounded_wait(0) == -1   # FWI_ERR_ARG
+    again = ctx.gradient(make_shots(shots), np.ascontiguousarray(obs, np.float32), mask)
+    assert again[0] == first[0]
+    for a, b in zip(again[1:], first[1:]):
+        assert np.array_equal(a, b)
