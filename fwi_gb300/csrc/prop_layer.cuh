@@ -10,7 +10,13 @@
 //   reference adjoint:  lP, lF + psi_xcx, psi_zdx (x-halo), psi_xcz, psi_zcz (z-halo)
 //
 // The zeta variables (read and written at each point only) load into
-// registers before the stage wait, like the increments.
+// registers before the stage wait, like the increments.  Where the tile
+// grid puts each band with the points beside it in one tile column or row
+// (TileGrid::inline_strip), the INLINE instantiations advance the memory
+// variables of their own band points in the tile instead of staging what the
+// strip pass wrote.  A layer group's shots share one window (their bands sit
+// at that window's edges); a thread polls each stage and the block meets
+// there (stage_ready), which measured faster here than per-thread waits.
 #pragma once
 
 #include "prop_tma.cuh"

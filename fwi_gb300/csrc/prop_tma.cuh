@@ -1,14 +1,17 @@
 // FP32 main passes (sm_103a): TMA tile loads, shot groups, 4-wide vectors.
 //
-// A 32 x 32 tile block loops over a group of shots that share a window.  Each
-// shot's halo'd fields arrive by cp.async.bulk.tensor into one of kStages
-// shared-memory stages while the block computes earlier shots (mbarrier
-// pipeline, one issuing thread); the increments and images, read at each
+// A 32 x 32 tile block loops over a group of shots (one window, or several:
+// the MIXED instantiations).  Each shot's halo'd fields arrive by
+// cp.async.bulk.tensor into one of kStages shared-memory stages while the
+// block computes earlier shots (mbarrier pipeline, one issuing thread; every
+// thread waits for its stage itself and the block meets where the stage is
+// handed back, stage_release); the increments and images, read at each
 // thread's own 4 points, are loaded into registers before the stage wait.  A
 // thread owns 4 consecutive points of a row: the x-stencil is 3
 // ld.shared.v4, the z-stencil 9, stores are 16-byte vectors.  The adjoint
-// sums the imaging of its group in registers (one gradient read-modify-write
-// per group and step).
+// sums the imaging of a one-window group in registers (one gradient
+// read-modify-write per group and step); a group of several windows adds
+// each shot's imaging to its own slot.
 //
 // These kernels take the interior tiles (tile_role 1: no point the CPML
 // layers touch); prop_layer.cuh takes the layer tiles.
