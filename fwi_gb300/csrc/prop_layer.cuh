@@ -282,8 +282,8 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
                 using SI = typename Cd::S;
                 SI *img = (SI *)b.store + sh.img;
                 SI eG[4], eH[4];
-#pragma unroll
                 bool sat = false;
+#pragma unroll
                 for (int q = 0; q < 4; q++) {
                     eG[q] = Cd::enc_flag(m[q] ? (EXACT ? G[q] : gP[q]) : 0.f, sh.sc, sat);
                     eH[q] = Cd::enc_flag(m[q] ? (EXACT ? H[q] : gF[q]) : 0.f, sh.sc, sat);

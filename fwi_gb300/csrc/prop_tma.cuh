@@ -358,8 +358,8 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
                 SI *img = (SI *)b.store + sh.img;
                 const float sc = sh.sc;
                 SI eG[4], eH[4];
-#pragma unroll
                 bool sat = false;
+#pragma unroll
                 for (int q = 0; q < 4; q++) {
                     eG[q] = Cd::enc_flag(m[q] ? gG[q] : 0.f, sc, sat);
                     eH[q] = Cd::enc_flag(m[q] ? gH[q] : 0.f, sc, sat);
