@@ -176,11 +176,28 @@ def cpu_sample(w, seconds=15.0, threads=None):
 
 # ----------------------------------------------------------------- GPU timing
 
+def image_bytes(store):
+    """Adjoint algorithmic bytes per point: 68 with FP32 images, 64 with 16-bit images
+    (the forward state the imaging reads is one FP16 / BF16 image pair, 4 B, not 8)."""
+    return ALG_BYTES_ADJ - (4 if store in ("fp16", "bf16") else 0)
+
+
+def config_of(args, w):
+    """The workload's `config` object, the same in both arms."""
+    nrec = max(s["rx1"] - s["rx0"] for s in w.shots)
+    ntr = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots)
+    return {"workload": w.name, "nx": w.nx, "nz": w.nz, "dh": w.dh, "dt": w.dt, "nt": w.nt,
+            "shots": len(w.shots), "receivers_per_shot": nrec, "ricker_hz": w.f, "cpml": w.cpml,
+            "mode": args.mode, "image_store": f"{args.storage}, {args.store}", "batch": args.batch,
+            "l2": f"inputs larger than L2 (observed data {ntr * 4 / 1e6:.0f} MB; the per-step state of "
+                  f"all shots {6 * 4 * w.nz * w.nx * len(w.shots) / 1e6:.0f} MB; images or rings streamed "
+                  f"through HBM)"}
+
+
 def native_arm(args, rank, world, dist):
     import torch
 
     import fwi_gb300
-    from fwi_gb300 import synth
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
@@ -189,133 +206,152 @@ def native_arm(args, rank, world, dist):
     mode = fwi_gb300.MODE_EXACT if args.mode == "exact" else fwi_gb300.MODE_REF_COMPAT
     sprec = {"fp32": fwi_gb300.SPREC_NATIVE, "fp16": fwi_gb300.SPREC_FP16, "bf16": fwi_gb300.SPREC_BF16}[args.store]
     nrec = max(s["rx1"] - s["rx0"] for s in w.shots)
-
-    storage = {"full": fwi_gb300.STORE_FULL, "checkpoint": fwi_gb300.STORE_CHECKPOINT,
-               "boundary": fwi_gb300.STORE_BOUNDARY}[args.storage]
+    store_of = {"full": fwi_gb300.STORE_FULL, "checkpoint": fwi_gb300.STORE_CHECKPOINT,
+                "boundary": fwi_gb300.STORE_BOUNDARY}
 
     # widest shot aperture (per-shot windows): per-shot arrays are sized by it, not by the model
     max_window = max((s["nxw"] or w.nx) for s in w.shots)
 
-    def context(max_shots, precision=fwi_gb300.PREC_FP32, store_prec=sprec, store=storage):
+    def context(max_shots, precision=fwi_gb300.PREC_FP32, store_prec=sprec, store=args.storage):
         c = fwi_gb300.Context(nx=w.nx, nz=w.nz, dh=w.dh, dt=w.dt, cpml=w.cpml, f_cpml=w.f, nt_max=w.nt,
                               max_shots=max_shots, max_receivers=nrec, max_window=max_window, mode=mode,
-                              precision=precision, store_prec=store_prec, store=store, device=dev)
+                              precision=precision, store_prec=store_prec, store=store_of[store], device=dev)
         c.set_ricker(w.f, w.nt)
         return c
 
-    # observed data from the true model, then the initial model
-    ctx = context(min(args.batch, len(w.shots)))
-    ctx.set_model(*w.squared())
+    # observed data from the true model (FP32, on the GPU); the runs then start from the initial model
     ntr = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots)
     obs_d = torch.zeros(ntr, dtype=torch.float32, device="cuda")
-    ctx.forward(shots, out=obs_d)
-    ctx.set_model(*w.squared(initial=True))
-    g_d = [torch.zeros((w.nz, w.nx), dtype=torch.float32, device="cuda") for _ in range(3)]
-    # launch choice: measured by the autotuner (before the warm-up, untimed) or the built-in one
-    tuning = ctx.autotune(shots, steps=args.autotune) if args.autotune > 0 else None
-
-    def step():
-        J, *_ = ctx.gradient(shots, obs_d, w.mask, out=g_d)
-        return J
-
-    ctx.set_tile_timing(True)  # events around the interior tile launches of sampled steps
-    for _ in range(args.warmup):
-        step()
-    clocks = Clocks()
-    barrier(dist)
-    torch.cuda.synchronize()
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches = 0
-    t_fwd = t_adj = t_tot = 0.0
-    tile = np.zeros(4)
-    e0.record()
-    for _ in range(args.steps):
-        J = step()
-        t = ctx.last_timing()
-        t_tot += float(t[0])
-        t_fwd += float(t[1])
-        t_adj += float(t[2])
-        tile += ctx.last_tile_timing() / args.steps
-        launches += ctx.last_launches()
-    e1.record()
-    torch.cuda.synchronize()
-    barrier(dist)
-    clk = clocks.stop(dev)
-    ms = e0.elapsed_time(e1) / args.steps
-    ms = max_over_ranks(dist, ms)
+    c0 = context(min(args.batch, len(w.shots)))
+    c0.set_model(*w.squared())
+    c0.forward(shots, out=obs_d)
+    del c0
+    hbm, peak_kind = peaks()
     nshots = len(w.shots)
-    upd = w.point_updates()
-    value = world * nshots / (ms / 1e3)
+    upd = w.physical_point_updates()
+    pts = sum(((s["nxw"] or w.nx) - 8) * (w.nz - 8) * s["nt"] for s in w.shots)  # updated points per phase
+    adj_bytes = image_bytes(args.store)
 
-    # end to end: pinned host observed data in, host gradients and misfit out
-    obs_h = obs_d.cpu().pin_memory()
-    g_h = [torch.zeros((w.nz, w.nx), dtype=torch.float32).pin_memory() for _ in range(3)]
-    for _ in range(2):
-        ctx.gradient(shots, obs_h, w.mask, out=g_h)
-    barrier(dist)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        ctx.gradient(shots, obs_h, w.mask, out=g_h)
-    torch.cuda.synchronize()
-    ms_e2e = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps)
-    barrier(dist)
+    def measure(storage, clocks_too):
+        """Gradient shots/s of the whole batch with `storage`: device-resident `value`, then e2e through
+        fwi_gradient with pinned host buffers."""
+        ctx = context(min(args.batch, len(w.shots)), store=storage)
+        ctx.set_model(*w.squared(initial=True))
+        g_d = [torch.zeros((w.nz, w.nx), dtype=torch.float32, device="cuda") for _ in range(3)]
+        # launch choice: measured by the autotuner (before the warm-up, untimed) or the built-in one
+        tuning = ctx.autotune(shots, steps=args.autotune) if args.autotune > 0 else None
 
-    out = None
-    if rank == 0:
-        hbm, peak_kind = peaks()
-        # dominant kernel: the adjoint interior tiles (k_adj_tma<.., LAYER=false>), the largest share of
-        # the launch list; per launch: algorithmic bytes (68 B per point update) of the interior points it
-        # updates / its mean duration, from CUDA events on its stream around sampled launches
+        def step():
+            J, *_ = ctx.gradient(shots, obs_d, w.mask, out=g_d)
+            return J
+
+        ctx.set_tile_timing(True)  # events around the interior tile launches of sampled steps
+        for _ in range(args.warmup):
+            step()
+        clocks = Clocks() if clocks_too else None
+        barrier(dist)
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches = 0
+        t_fwd = t_adj = t_tot = 0.0
+        tile = np.zeros(4)
+        e0.record()
+        for _ in range(args.steps):
+            J = step()
+            t = ctx.last_timing()
+            t_tot += float(t[0])
+            t_fwd += float(t[1])
+            t_adj += float(t[2])
+            tile += ctx.last_tile_timing() / args.steps
+            launches += ctx.last_launches()
+        e1.record()
+        torch.cuda.synchronize()
+        barrier(dist)
+        clk = clocks.stop(dev) if clocks else None
+        ms = max_over_ranks(dist, e0.elapsed_time(e1) / args.steps)
+
+        # end to end: pinned host observed data in, host gradients and misfit out
+        obs_h = obs_d.cpu().pin_memory()
+        g_h = [torch.zeros((w.nz, w.nx), dtype=torch.float32).pin_memory() for _ in range(3)]
+        for _ in range(2):
+            ctx.gradient(shots, obs_h, w.mask, out=g_h)
+        barrier(dist)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.gradient(shots, obs_h, w.mask, out=g_h)
+        torch.cuda.synchronize()
+        ms_e2e = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps)
+        barrier(dist)
+        del ctx
+        # dominant kernel: the adjoint interior tiles (the largest share of the launch list); per launch:
+        # algorithmic bytes of the interior points it updates / its mean duration, from CUDA events on its
+        # stream around sampled launches
         adj_ms, adj_pts = float(tile[2]), float(tile[3])
         fwd_ms, fwd_pts = float(tile[0]), float(tile[1])
-        kern_gbs = ALG_BYTES_ADJ * adj_pts / (adj_ms / 1e3) / 1e9 if adj_ms > 0 else None
+        kern_gbs = adj_bytes * adj_pts / (adj_ms / 1e3) / 1e9 if adj_ms > 0 else None
         fwd_kern_gbs = ALG_BYTES_FWD * fwd_pts / (fwd_ms / 1e3) / 1e9 if fwd_ms > 0 else None
-        # whole phases (all kernels of a step, every point), timed on the context stream
-        pts = sum((s["nxw"] or w.nx) * w.nz * s["nt"] for s in w.shots)
-        adj_gbs = ALG_BYTES_ADJ * pts / (t_adj / args.steps / 1e3) / 1e9
-        fwd_gbs = ALG_BYTES_FWD * pts / (t_fwd / args.steps / 1e3) / 1e9
-        traffic = traffic_from_profile(f"k_adj_tma_interior_{args.workload}.txt")
-        out = {
-            "metric": METRIC, "value": round(value, 4), "unit": "shots/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": f"synthetic (seeded {args.workload} model, observed data modelled on the GPU from the true model)",
-            "config": {"workload": w.name, "nx": w.nx, "nz": w.nz, "dh": w.dh, "dt": w.dt, "nt": w.nt,
-                       "shots": nshots, "receivers_per_shot": nrec, "ricker_hz": w.f, "cpml": w.cpml,
-                       "mode": args.mode, "image_store": f"{args.storage}, {args.store}", "batch": args.batch,
-                       "launch_choice": ({k: (round(v, 2) if isinstance(v, float) else v) for k, v in tuning.items()}
-                                         | {"by": f"fwi_autotune, {args.autotune} steps per candidate"}
-                                         if tuning else "built-in"),
-                       "l2": f"inputs larger than L2 (observed data {ntr * 4 / 1e6:.0f} MB; the per-step state of "
-                             f"all shots {6 * 4 * w.nz * w.nx * nshots / 1e6:.0f} MB; images or rings streamed "
-                             f"through HBM)"},
+        r = {
+            "value": round(world * nshots / (ms / 1e3), 4), "ms_per_step": round(ms, 3), "misfit": J,
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
                     "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
             "roofline": {"bound": "hbm", "kernel": "k_adj_tma interior tiles (adjoint step + imaging)",
                          "achieved": round(kern_gbs, 1) if kern_gbs else None, "peak": hbm, "unit": "GB/s",
                          "frac": round(kern_gbs / hbm, 4) if kern_gbs else None, "peak_kind": peak_kind,
-                         "traffic": traffic,
+                         "traffic": traffic_from_profile(f"k_adj_tma_interior_{args.workload}.txt"),
                          "launch_ms": round(adj_ms, 4), "points_per_launch": int(adj_pts),
-                         "bytes_per_point": ALG_BYTES_ADJ,
+                         "bytes_per_point": adj_bytes,
                          "forward_interior": {"achieved": round(fwd_kern_gbs, 1) if fwd_kern_gbs else None,
                                               "frac": round(fwd_kern_gbs / hbm, 4) if fwd_kern_gbs else None,
                                               "launch_ms": round(fwd_ms, 4), "points_per_launch": int(fwd_pts),
                                               "bytes_per_point": ALG_BYTES_FWD},
-                         "adjoint_step_frac": round(adj_gbs / hbm, 4),
-                         "forward_step_frac": round(fwd_gbs / hbm, 4),
-                         "gradient_frac": round((ALG_BYTES_FWD + ALG_BYTES_ADJ) * pts / (t_tot / args.steps / 1e3)
+                         # whole phases (all kernels of a step, every updated point), on the context stream
+                         "adjoint_step_frac": round(adj_bytes * pts / (t_adj / args.steps / 1e3) / 1e9 / hbm, 4),
+                         "forward_step_frac": round(ALG_BYTES_FWD * pts / (t_fwd / args.steps / 1e3) / 1e9 / hbm, 4),
+                         # the survey's point-update basis: useful updates x 52 B (36 + 68, two updates)
+                         "gradient_frac": round(world * upd / (ms / 1e3) * (ALG_BYTES_FWD + ALG_BYTES_ADJ) / 2
                                                 / 1e9 / hbm, 4)},
             "gpu_launches": int(launches),
             "phase_ms": {"forward": round(t_fwd / args.steps, 3), "adjoint": round(t_adj / args.steps, 3),
                          "other": round((t_tot - t_fwd - t_adj) / args.steps, 3)},
-            "misfit": J,
+            "launch_choice": ({k: (round(v, 2) if isinstance(v, float) else v) for k, v in tuning.items()}
+                              | {"by": f"fwi_autotune, {args.autotune} steps per candidate"}
+                              if tuning else "built-in"),
         }
         if clk:
-            out["clocks"] = clk
-    del ctx
+            r["clocks"] = clk
+        return r
+
+    head = measure(args.storage, True)
+    out = None
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": head["value"], "unit": "shots/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": f"synthetic (seeded {args.workload} model, observed data modelled on the GPU from the true model)",
+            "config": config_of(args, w), "launch_choice": head["launch_choice"],
+            "gpt_updates_per_s": head["gpt_updates_per_s"],
+            "gpt_updates_counted_on": f"updated points: {w.nx - 8} x {w.nz - 8} per shot and step, forward and "
+                                      f"adjoint (the 4-point frame excluded)",
+            "e2e": head["e2e"], "roofline": head["roofline"], "gpu_launches": head["gpu_launches"],
+            "phase_ms": head["phase_ms"], "misfit": head["misfit"],
+        }
+        if "clocks" in head:
+            out["clocks"] = head["clocks"]
+
+    if not args.skip_extras:
+        # the other image stores, same workload and timing rules
+        for other in [s for s in ("checkpoint", "full") if s != args.storage]:
+            o = measure(other, False)
+            if rank == 0:
+                out.setdefault("other_storage", {})[other] = {
+                    k: o[k] for k in ("value", "ms_per_step", "gpt_updates_per_s", "phase_ms", "launch_choice")
+                } | {"e2e": o["e2e"]["value"], "roofline_frac": o["roofline"]["frac"],
+                     "gradient_frac": o["roofline"]["gradient_frac"]}
 
     if rank == 0 and not args.skip_extras:
         # plain per-shot FP32 path (one shot per launch sequence, FP32 images, every step's kernels
@@ -325,7 +361,7 @@ def native_arm(args, rank, world, dist):
         nsub = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots[: args.plain_shots])
         plain = {}
         for graphs in (False, True):
-            c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE)
+            c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE, store="full")
             c1.set_graphs(graphs)
             c1.set_model(*w.squared(initial=True))
             for _ in range(2):
@@ -335,40 +371,27 @@ def native_arm(args, rank, world, dist):
             c1.gradient(sub, obs_d[:nsub])
             torch.cuda.synchronize()
             plain[graphs] = args.plain_shots / (time.perf_counter() - t0)
-            if not graphs:
-                ref32 = c1.gradient(sub, obs_d[:nsub].cpu().numpy())
             del c1
+        value = out["value"] / world
         out["plain_gpu"] = {"value": round(plain[False], 4), "unit": "shots/s",
-                            "how": f"max_shots=1, FP32 images, {args.storage} storage, kernels launched from the "
-                                   f"host every step, {args.plain_shots} shots timed",
-                            "speedup": round(value / world / plain[False], 2),
+                            "how": f"max_shots=1, FP32 images, full storage, kernels launched from the host "
+                                   f"every step, {args.plain_shots} shots timed",
+                            "speedup": round(value / plain[False], 2),
                             "with_graph_replay": {"value": round(plain[True], 4),
-                                                  "speedup": round(value / world / plain[True], 2)}}
-        # gradient error of this configuration against the FP64 GPU path, same shots and storage
-        c64 = context(args.plain_shots, precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE)
-        c64.set_model(*(a.astype(np.float64) for a in w.squared(initial=True)))
-        r64 = c64.gradient(sub, obs_d[:nsub].cpu().numpy().astype(np.float64))
-        del c64
-        cx = context(args.plain_shots)
-        cx.set_model(*w.squared(initial=True))
-        rx = cx.gradient(sub, obs_d[:nsub].cpu().numpy())
-        del cx
-        rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
-        out["grad_rel_err_vs_fp64"] = {
-            "this_config": [round(rel(a, b), 7) for a, b in zip(rx[1:], r64[1:])],
-            "fp32_images": [round(rel(a, b), 7) for a, b in zip(ref32[1:], r64[1:])],
-            "order": "v_hor, v_po, v_nmo", "shots": args.plain_shots,
-            "misfit_rel_err": abs(rx[0] - r64[0]) / abs(r64[0])}
+                                                  "speedup": round(value / plain[True], 2)}}
+        for k, o in out.get("other_storage", {}).items():
+            o["plain_gpu_speedup"] = round(o["value"] / world / plain[False], 2)
+        out["accuracy_vs_fp64"] = accuracy(args, w, context, obs_d, fwi_gb300)
         # L-BFGS two-loop (m = 5) on this grid, FP64 dots
-        from fwi_gb300 import Context
         cl = context(1)
         cl.set_model(*w.squared(initial=True))
-        cl.set_gradient(*(a.astype(np.float32) for a in r64[1:]))
-        cl.first_step(3e5, 2e5, 2.5e5)
         rng = np.random.default_rng(0)
+        g0 = [rng.standard_normal((w.nz, w.nx)).astype(np.float32) for _ in range(3)]
+        cl.set_gradient(*g0)
+        cl.first_step(3e5, 2e5, 2.5e5)
         for it in range(6):
-            cl.set_gradient(*(a.astype(np.float32) * (1 + 0.01 * it) + rng.standard_normal(a.shape).astype(np.float32)
-                              * 1e-3 * float(np.abs(a).max()) for a in r64[1:]))
+            cl.set_gradient(*(a * (1 + 0.01 * it) + rng.standard_normal(a.shape).astype(np.float32) * 1e-3
+                              for a in g0))
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             cl.lbfgs_direction(5)
@@ -376,11 +399,72 @@ def native_arm(args, rank, world, dist):
             cl.lbfgs_update(1e-3, 1e-3, 1e-3)
         out["lbfgs_direction_ms"] = round(tl * 1e3, 3)
         del cl
+        if args.invert_iters > 0:
+            out["inversion"] = inversion(args, w, context, obs_d, shots, torch)
     if rank == 0 and not args.skip_cpu:
         v, thr, sample = cpu_sample(w, seconds=args.cpu_seconds)
         out["cpu_baseline"] = {"value": round(v, 6), "unit": "shots/s", "cores": thr, "kind": "port",
                                "sample": sample}
+        v1, _, sample1 = cpu_sample(w, seconds=args.cpu_seconds, threads=1)
+        out["cpu_baseline_single_thread"] = {"value": round(v1, 6), "unit": "shots/s", "cores": 1, "kind": "port",
+                                             "sample": sample1}
     return out
+
+
+def accuracy(args, w, context, obs_d, fwi_gb300):
+    """Residual, misfit and gradient errors of this configuration (storage, image type) against the FP64 GPU
+    path on the first shots, same observed data.  Gradients compare over the whole grid and over the rows
+    the model update changes (below the near-surface layer of 15 rows, src/parallelcalls.cu:343-404)."""
+    n = args.accuracy_shots
+    sub = fwi_gb300.make_shots(w.shots[:n])
+    nsub = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots[:n])
+    obs32 = obs_d[:nsub].cpu().numpy()
+    mask = None if w.mask is None else w.mask[: sum(s["rx1"] - s["rx0"] for s in w.shots[:n])]
+    c64 = context(min(n, args.batch), precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE,
+                  store="full")
+    c64.set_model(*(a.astype(np.float64) for a in w.squared(initial=True)))
+    r64 = c64.gradient(sub, obs32.astype(np.float64), mask)
+    syn64 = c64.forward(sub)
+    del c64
+    out = {"shots": n, "order": "v_hor, v_po, v_nmo", "update_rows": "iz > 15"}
+    rel = lambda a, b, z=0: float(np.linalg.norm((a - b)[z:]) / np.linalg.norm(b[z:]))
+    res64 = syn64 - obs32.astype(np.float64)
+    for label, store, sp in ((f"{args.storage}_{args.store}", args.storage, None),
+                             ("full_fp32_images", "full", fwi_gb300.SPREC_NATIVE)):
+        cx = context(min(n, args.batch), store=store, **({} if sp is None else {"store_prec": sp}))
+        cx.set_model(*w.squared(initial=True))
+        rx = cx.gradient(sub, obs32, mask)
+        syn32 = cx.forward(sub)
+        del cx
+        out[label] = {
+            "gradient": [round(rel(a, b), 7) for a, b in zip(rx[1:], r64[1:])],
+            "gradient_update_rows": [round(rel(a, b, 16), 7) for a, b in zip(rx[1:], r64[1:])],
+            "residual": round(float(np.linalg.norm(syn32 - obs32 - res64) / np.linalg.norm(res64)), 9),
+            "traces": round(float(np.linalg.norm(syn32 - syn64) / np.linalg.norm(syn64)), 9),
+            "misfit": abs(rx[0] - r64[0]) / abs(r64[0])}
+    g = r64[1:]
+    out["gradient_norm_share_in_rows_0_15"] = [round(float(np.sum(a[:16] ** 2) / np.sum(a ** 2)), 4) for a in g]
+    return out
+
+
+def inversion(args, w, context, obs_d, shots, torch):
+    """The workload's inversion loop through the C driver (fwi_invert: steepest first step, then L-BFGS
+    with the backtracking line search, src/main.c:396-801) from the initial model, timed end to end."""
+    ctx = context(min(args.batch, len(w.shots)))
+    ctx.set_model(*w.squared(initial=True))
+    if args.autotune > 0:
+        ctx.autotune(shots, steps=args.autotune)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = ctx.invert(shots, obs_d, w.mask, iterations=args.invert_iters, lbfgs_m=5)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    del ctx
+    return {"iterations": len(hist), "requested": args.invert_iters, "lbfgs_m": 5, "storage": args.storage,
+            "wall_s": round(dt, 3), "s_per_iteration": round(dt / max(1, len(hist)), 4),
+            "misfit_first": float(hist[0]) if len(hist) else None,
+            "misfit_last": float(hist[-1]) if len(hist) else None,
+            "misfit_history": [float(x) for x in hist]}
 
 
 def reference_arm(args, rank, world, dist):
@@ -402,8 +486,7 @@ def reference_arm(args, rank, world, dist):
     return {"metric": METRIC, "value": round(v, 6), "unit": "shots/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "impl": "reference",
-            "data": "synthetic", "config": {"workload": w.name, "nx": w.nx, "nz": w.nz, "nt": w.nt,
-                                            "shots": len(w.shots)},
+            "data": f"synthetic (seeded {args.workload} model)", "config": config_of(args, w),
             "cpu_baseline": {"value": round(v, 6), "unit": "shots/s", "cores": thr, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(v, 6), "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -421,9 +504,12 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--mode", default="exact", choices=["exact", "ref"])
     ap.add_argument("--store", default="fp16", choices=["fp32", "fp16", "bf16"])
-    ap.add_argument("--storage", default="full", choices=["full", "checkpoint", "boundary"],
-                    help="how the forward images are kept (FWI_STORE_*)")
+    ap.add_argument("--storage", default="checkpoint", choices=["full", "checkpoint", "boundary"],
+                    help="how the forward images are kept (FWI_STORE_*) in the headline run")
     ap.add_argument("--plain-shots", type=int, default=4)
+    ap.add_argument("--accuracy-shots", type=int, default=8, help="shots of the FP64 comparison")
+    ap.add_argument("--invert-iters", type=int, default=20,
+                    help="L-BFGS iterations of the timed inversion loop (0: none)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-extras", action="store_true")

@@ -22,7 +22,6 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libfwi_gb300.so")
 
 UNITS = ["compat.cu", "native.cu", "prop_f32.cu", "prop_f64.cu", "noalloc.cu"]
-HEADERS = ["common.cuh", "tile.cuh", "prop.h", "prop.cuh", "prop_tma.cuh", "tma.cuh"]
 C_UNITS = ["driver.c"]  # host C over the C-ABI
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -39,22 +38,41 @@ def _stale(target: str, deps) -> bool:
     if not os.path.exists(target):
         return True
     t = os.path.getmtime(target)
-    return any(os.path.getmtime(d) > t for d in deps)
+    return any(not os.path.exists(d) or os.path.getmtime(d) > t for d in deps)
+
+
+def _depfile_deps(dep: str):
+    """Prerequisites listed in a make-style dependency file (nvcc / gcc -MD), or None."""
+    try:
+        text = open(dep).read()
+    except OSError:
+        return None
+    text = text.replace("\\\n", " ")
+    _, _, rhs = text.partition(":")
+    return [d for d in rhs.split() if d != "\\"]
+
+
+def _deps(src: str, obj: str, local_headers):
+    """Every header the last compile of `src` read (from its -MD file), else all local headers."""
+    listed = _depfile_deps(obj[:-2] + ".d")
+    return [src] + (listed if listed is not None else local_headers)
 
 
 def build(force: bool = False, jobs: int = 4, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     inc = os.path.join(os.path.dirname(PKG), "include")
-    headers = [os.path.join(CSRC, h) for h in HEADERS] + [
+    # without a dependency file (first build), any local header counts
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))] + [
         os.path.join(inc, h) for h in os.listdir(inc) if h.endswith(".h")]
     objs, todo = [], []
     for u in UNITS:
         src = os.path.join(CSRC, u)
         obj = os.path.join(BUILD, u.replace(".cu", ".o"))
         objs.append(obj)
-        if force or _stale(obj, [src] + headers):
-            todo.append([nvcc(), *ARCH, *NVCC_FLAGS, "-I", inc, "-c", src, "-o", obj])
+        if force or _stale(obj, _deps(src, obj, headers)):
+            todo.append([nvcc(), *ARCH, *NVCC_FLAGS, "-I", inc, "-MD", "-MF", obj[:-2] + ".d", "-c", src,
+                         "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -69,8 +87,9 @@ def build(force: bool = False, jobs: int = 4, verbose: bool = False) -> str:
         src = os.path.join(CSRC, u)
         obj = os.path.join(BUILD, u.replace(".c", ".o"))
         objs.append(obj)
-        if force or _stale(obj, [src] + headers):
-            todo.append([cc, "-O2", "-fPIC", "-std=c11", "-Wall", "-I", inc, "-c", src, "-o", obj])
+        if force or _stale(obj, _deps(src, obj, headers)):
+            todo.append([cc, "-O2", "-fPIC", "-std=c11", "-Wall", "-I", inc, "-MD", "-MF", obj[:-2] + ".d",
+                         "-c", src, "-o", obj])
 
     with ThreadPoolExecutor(max_workers=max(1, jobs)) as ex:
         list(ex.map(run, todo))

@@ -499,10 +499,19 @@ __global__ void k_update_lbfgs(const float *r1, const float *r2, const float *r3
 }
 
 constexpr int kEltBlock = 256;
+// Grid of a grid-stride kernel: one block per kEltBlock elements, at most 16
+// blocks per SM of the current device (the runtime caches the attribute).
 inline unsigned elt_grid(long n)
 {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        sms = 1;
+    }
+    const long cap = 16L * sms;
     long b = (n + kEltBlock - 1) / kEltBlock;
-    return (unsigned)(b < 152L * 16 ? (b > 0 ? b : 1) : 152L * 16);
+    return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
 }  // namespace

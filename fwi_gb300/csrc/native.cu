@@ -89,8 +89,7 @@ int status_from_cuda(cudaError_t e)
 
 constexpr int kLayer = 15;  // near-surface rows never updated (include/parallelcalls.h:6)
 constexpr int kMaxHist = 16;
-constexpr int kRedBlocks = 304;  // reduction grid: 2 blocks per SM of a 152-SM GB300
-constexpr int kRedThreads = 256;
+constexpr int kRedThreads = 256;  // reduction grids: 2 blocks of kRedThreads per SM of the device
 
 long round_up(long v, long m) { return (v + m - 1) / m * m; }
 
@@ -214,7 +213,7 @@ __global__ void k_accumulate_gradient(T *gh, T *gp, T *gn, const T *sh_h, const 
 
 // Three-parameter dot products with a last-block-done FP64 reduction.
 struct DotScratch {
-    double *partial;    // [kRedBlocks][4][3]
+    double *partial;    // [reduction blocks][4][3]
     unsigned *counter;  // one per kernel sequence position
 };
 
@@ -437,10 +436,11 @@ int checkpoint_interval(const fwi_config &c)
     return std::max(1, std::min(k, c.nt_max));
 }
 
-inline unsigned elt_grid(long n)
+// Grid of a grid-stride element-wise kernel of 256-thread blocks: at most 8 blocks per SM.
+inline unsigned elt_grid(long n, int n_sm)
 {
     long b = (n + 255) / 256;
-    return (unsigned)std::max(1L, std::min(b, 152L * 8));
+    return (unsigned)std::max(1L, std::min(b, 8L * n_sm));
 }
 
 // Check of the bounded pipeline wait (fwi_check_bounded_wait): one block
@@ -472,6 +472,9 @@ struct NvtxRange {
 struct CtxBase {
     fwi_config cfg{};
     int last_cuda = 0;
+    int n_sm = 1;        // streaming multiprocessors of the context's device
+    int red_blocks = 2;  // blocks of the reduction kernels: 2 per SM
+    unsigned eg(long n) const { return elt_grid(n, n_sm); }
     float timing[4] = {0, 0, 0, 0};
     long launches = 0;
 
@@ -783,6 +786,8 @@ template <typename T> struct Ctx : CtxBase {
         mslot = (long)nz * mpitch;
         n_img = nt_max;
         TRY(cudaSetDevice(cfg.device));
+        TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, cfg.device));
+        red_blocks = 2 * n_sm;
         if (const char *e = getenv("FWI_GRAPHS")) graphs = atoi(e) != 0;
         TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         for (auto &e : ev) TRY(cudaEventCreate(&e));
@@ -860,13 +865,13 @@ template <typename T> struct Ctx : CtxBase {
         TRY(alloc(&mask_off, B));
         TRY(alloc(&shots, B));
         TRY(alloc(&status, 1));
-        TRY(alloc(&partial, (size_t)B * kRedBlocks));
+        TRY(alloc(&partial, (size_t)B * red_blocks));
         TRY(alloc(&misfit, 1));
         for (auto &p : grad) TRY(alloc(&p, mslot));
         for (T **p : {&mb[0], &mb[1], &mb[2], &gb[0], &gb[1], &gb[2], &q[0], &q[1], &q[2], &r[0], &r[1], &r[2]})
             TRY(alloc(p, mslot));
         TRY(alloc(&lbs, 1));
-        TRY(alloc(&ds.partial, (size_t)kRedBlocks * 12));
+        TRY(alloc(&ds.partial, (size_t)red_blocks * 12));
         TRY(alloc(&ds.counter, 1));
         TRY(cudaMemsetAsync(ds.counter, 0, sizeof(unsigned), st));
         TRY(cudaMemsetAsync(lbs, 0, sizeof(LbScalars), st));
@@ -905,7 +910,7 @@ template <typename T> struct Ctx : CtxBase {
     // block).  The tile passes are latency-bound, so many short blocks beat
     // few long ones: the
     // group count gives about three waves of adjoint tile blocks (3 resident
-    // per SM of a 152-SM GB300).  Measured on 601 x 301, 32 shots: 5 shots
+    // per SM).  Measured on 601 x 301, 32 shots: 5 shots
     // per group (7 groups) 56.8 shots/s, 8: 53.8, 3: 52.3, 16: 40.6.
     static bool uniform_windows(const std::vector<DevShot> &bs)
     {
@@ -922,7 +927,7 @@ template <typename T> struct Ctx : CtxBase {
             if (v >= 1) return std::min(v, 64);
         }
         const long tiles = (long)((nxm - 5) / 32 + 1) * ((nz - 5) / 32 + 1);  // tiles holding interior points
-        const long slots = 3L * 152;
+        const long slots = 3L * n_sm;
         const long nb = (long)bs.size();
         const long groups = std::max(1L, std::min(nb, (3 * slots + tiles / 2) / tiles));
         const long sg = (nb + groups - 1) / groups;
@@ -931,7 +936,7 @@ template <typename T> struct Ctx : CtxBase {
 
     // Shots per group of the layer tiles (with identical windows).  They run
     // on the side stream beside the interior tiles; the group count gives
-    // about half a wave of adjoint blocks (3 per SM of 152): short enough a
+    // about half a wave of adjoint blocks (3 per SM): short enough a
     // pass, without a block prologue per shot.  Measured on 601 x 301, 32
     // shots (54 layer tiles): 8 shots per group 60.2 shots/s, 5: 59.1,
     // 16: 54.9, 2: 56.6, 1: 53.4.
@@ -945,7 +950,7 @@ template <typename T> struct Ctx : CtxBase {
         for (int z0 = zbase; z0 < nz; z0 += fwi::kTileEdge)
             for (int x0 = xbase; x0 < nxm; x0 += fwi::kTileEdge)
                 tiles += fwi::tile_role(x0, z0, nxm, nz, cfg.cpml + fwi::kRad) == 2;
-        const long slots = 3L * 152 / 2;
+        const long slots = 3L * n_sm / 2;
         const long groups = std::max(1L, std::min((long)nb, (slots + tiles / 2) / std::max(1L, tiles)));
         return (int)std::max(1L, std::min((nb + groups - 1) / groups, 64L));
     }
@@ -1074,7 +1079,7 @@ template <typename T> struct Ctx : CtxBase {
         TRY(cudaMemcpyAsync(grad[0], vel, bytes, cudaMemcpyDefault, st));
         TRY(cudaMemcpyAsync(grad[1], eps, bytes, cudaMemcpyDefault, st));
         TRY(cudaMemcpyAsync(grad[2], del, bytes, cudaMemcpyDefault, st));
-        k_pre_variables<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(grad[0], grad[1], grad[2], vh, vp, vn, nx,
+        k_pre_variables<T><<<eg((long)nx * nz), 256, 0, st>>>(grad[0], grad[1], grad[2], vh, vp, vn, nx,
                                                                      nz, mpitch);
         TRY_LAUNCH();
         launches++;
@@ -1126,7 +1131,7 @@ template <typename T> struct Ctx : CtxBase {
     {
         if (!models_dirty) return FWI_OK;
         const T dt2 = (T)cfg.dt * (T)cfg.dt;
-        k_scale_models<T><<<elt_grid(mslot), 256, 0, st>>>(vh, vp, vn, mh, mp, mn, dt2, mslot);
+        k_scale_models<T><<<eg(mslot), 256, 0, st>>>(vh, vp, vn, mh, mp, mn, dt2, mslot);
         TRY_LAUNCH();
         launches++;
         models_dirty = false;
@@ -1320,9 +1325,9 @@ template <typename T> struct Ctx : CtxBase {
             if (rc) return rc;
             TRY(cudaEventRecord(e1, st));
             if (obs_in) {
-                k_residual<T><<<dim3(kRedBlocks, nb), kRedThreads, 0, st>>>(rec, obs, mask_in ? mask : nullptr, shots,
+                k_residual<T><<<dim3(red_blocks, nb), kRedThreads, 0, st>>>(rec, obs, mask_in ? mask : nullptr, shots,
                                                                           mask_off, partial);
-                k_misfit_finish<<<1, 256, 0, st>>>(partial, (long)nb * kRedBlocks, misfit);
+                k_misfit_finish<<<1, 256, 0, st>>>(partial, (long)nb * red_blocks, misfit);
                 TRY_LAUNCH();
                 launches += 2;
             }
@@ -1450,7 +1455,7 @@ template <typename T> struct Ctx : CtxBase {
                         }
                         TRY_LAUNCH();
                     }
-                    k_accumulate_gradient<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(
+                    k_accumulate_gradient<T><<<eg((long)nx * nz), 256, 0, st>>>(
                         grad[0], grad[1], grad[2], gs[0], gs[1], gs[2], shots, nslots, 1, nx, nz, mpitch, pitch, slot);
                     TRY_LAUNCH();
                     launches++;
@@ -1752,9 +1757,9 @@ template <typename T> struct Ctx : CtxBase {
         if ((rc = copy3(mb, m3)) || (rc = copy3(gb, grad))) return rc;
         have_back = true;
         // |g|^2 over the whole grid (src/main.c:551-559), in FP64
-        k_lb_copy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(q), ctri(grad), ctri(grad), mslot, ds, lbs->dots);
+        k_lb_copy_dot<T><<<red_blocks, kRedThreads, 0, st>>>(tri(q), ctri(grad), ctri(grad), mslot, ds, lbs->dots);
         k_lb_inv_norm<<<1, 32, 0, st>>>(lbs);
-        k_first_update<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(vh, vp, vn, grad[0], grad[1], grad[2], lbs, a_hor,
+        k_first_update<T><<<eg((long)nx * nz), 256, 0, st>>>(vh, vp, vn, grad[0], grad[1], grad[2], lbs, a_hor,
                                                                    a_po, a_nmo, nx, nz, mpitch);
         TRY_LAUNCH();
         launches += 3;
@@ -1789,7 +1794,7 @@ template <typename T> struct Ctx : CtxBase {
         const int k = hist_next % m;
         T *sk[3] = {hs[k][0], hs[k][1], hs[k][2]}, *yk[3] = {hy[k][0], hy[k][1], hy[k][2]};
         T *m3[3] = {vh, vp, vn};
-        k_lb_pair<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(sk), tri(yk), ctri(m3), ctri(mb), ctri(grad), ctri(gb),
+        k_lb_pair<T><<<red_blocks, kRedThreads, 0, st>>>(tri(sk), tri(yk), ctri(m3), ctri(mb), ctri(grad), ctri(gb),
                                                          mslot, ds, lbs->pair);
         hist_next = (hist_next + 1) % m;
         hist_count = std::min(hist_count + 1, m);
@@ -1808,7 +1813,7 @@ template <typename T> struct Ctx : CtxBase {
             const bool has_next = a + 1 < order.size();
             const int ln = has_next ? order[a + 1] : l;
             T *sn[3] = {hs[ln][0], hs[ln][1], hs[ln][2]};
-            k_lb_axpy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(q), ctri(yl), nullptr, lbs->coefB, ctri(sn),
+            k_lb_axpy_dot<T><<<red_blocks, kRedThreads, 0, st>>>(tri(q), ctri(yl), nullptr, lbs->coefB, ctri(sn),
                                                                  has_next ? 1 : 0, mslot, ds, lbs->dots);
         }
         // r = gamma q; then the second loop oldest .. newest
@@ -1817,7 +1822,7 @@ template <typename T> struct Ctx : CtxBase {
         T *y0[3] = {hy[first][0], hy[first][1], hy[first][2]};
         rcq = copy3(r, q);
         if (rcq) return rcq;
-        k_lb_axpy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(r), cnull(), lbs->coefA, nullptr, ctri(y0), 1, mslot,
+        k_lb_axpy_dot<T><<<red_blocks, kRedThreads, 0, st>>>(tri(r), cnull(), lbs->coefA, nullptr, ctri(y0), 1, mslot,
                                                              ds, lbs->dots);
         for (int a = (int)order.size() - 1; a >= 0; a--) {
             const int l = order[a];
@@ -1826,7 +1831,7 @@ template <typename T> struct Ctx : CtxBase {
             const bool has_next = a > 0;
             const int ln = has_next ? order[a - 1] : l;
             T *yn[3] = {hy[ln][0], hy[ln][1], hy[ln][2]};
-            k_lb_axpy_dot<T><<<kRedBlocks, kRedThreads, 0, st>>>(tri(r), ctri(sl), nullptr, lbs->coefB, ctri(yn),
+            k_lb_axpy_dot<T><<<red_blocks, kRedThreads, 0, st>>>(tri(r), ctri(sl), nullptr, lbs->coefB, ctri(yn),
                                                                  has_next ? 1 : 0, mslot, ds, lbs->dots);
         }
         TRY_LAUNCH();
@@ -1851,7 +1856,7 @@ template <typename T> struct Ctx : CtxBase {
     int direction_slope(double *out3) override
     {
         if (!have_dir) return FWI_ERR_STATE;
-        k_lb_slope<T><<<kRedBlocks, kRedThreads, 0, st>>>(ctri(gb), ctri(r), nx, nz, mpitch, ds, lbs->dots);
+        k_lb_slope<T><<<red_blocks, kRedThreads, 0, st>>>(ctri(gb), ctri(r), nx, nz, mpitch, ds, lbs->dots);
         TRY_LAUNCH();
         launches++;
         double d[3];
@@ -1865,7 +1870,7 @@ template <typename T> struct Ctx : CtxBase {
     {
         if (!have_back) return FWI_ERR_STATE;
         // av, ad, ae pair with (v_po, v_nmo, v_hor) as update_LBFGS does (src/main.c:693)
-        k_lb_update<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(vh, vp, vn, mb[0], mb[1], mb[2], r[0], r[1], r[2], av,
+        k_lb_update<T><<<eg((long)nx * nz), 256, 0, st>>>(vh, vp, vn, mb[0], mb[1], mb[2], r[0], r[1], r[2], av,
                                                                 ad, ae, fmin, fmax, nx, nz, mpitch);
         TRY_LAUNCH();
         launches++;
@@ -1901,7 +1906,7 @@ template <typename T> struct Ctx : CtxBase {
         if (!have_grad) return FWI_ERR_STATE;
         for (auto &p : vti_out)
             if (!p) TRY(alloc(&p, mslot));
-        k_grad_vti<T><<<elt_grid((long)nx * nz), 256, 0, st>>>(vh, vp, vn, grad[0], grad[1], grad[2], vti_out[0],
+        k_grad_vti<T><<<eg((long)nx * nz), 256, 0, st>>>(vh, vp, vn, grad[0], grad[1], grad[2], vti_out[0],
                                                                vti_out[1], vti_out[2], nx, nz, mpitch);
         TRY_LAUNCH();
         void *outs[3] = {o0, o1, o2};

@@ -17,13 +17,10 @@ namespace {
 
 constexpr int kChunk = 4096;     // elements each block reduces (fixed, so the sum order is too)
 constexpr int kThreads = 256;
-constexpr int kMaxDevices = 64;
 
 // Per-block FP64 partial sums, then the completion counter in the last slot.
 // Every GPU that loads the library holds this array (128 KiB + 8 B) until exit.
 static __device__ __align__(256) double g_scratch[FWI_NOALLOC_MAX_BLOCKS + 1];
-
-double *g_scratch_addr[kMaxDevices] = {};
 
 __global__ void k_residual_noalloc(float *res, const float *__restrict__ syn, const float *__restrict__ obs,
                                    const unsigned char *__restrict__ mask, long n, int nrec, double *scratch,
@@ -61,23 +58,25 @@ __global__ void k_residual_noalloc(float *res, const float *__restrict__ syn, co
     *(unsigned *)&scratch[FWI_NOALLOC_MAX_BLOCKS] = 0u;
 }
 
-// Device address of the scratch array for the current device (looked up on
-// the first call on each device; a host-side name is not a device address).
+// Device address of the scratch array on the current device.  The host-side
+// name g_scratch is not a device address, so it is looked up with the device
+// current, on every call: a host-side table lookup once the module is loaded
+// there, and never stale (after cudaDeviceReset the module loads again,
+// possibly at another address) nor shared between host threads.
 int scratch_for_current_device(double **out)
 {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return FWI_ERR_NODEVICE;
-    if (dev < 0 || dev >= kMaxDevices) return FWI_ERR_UNSUPPORTED;
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return e == cudaErrorNoKernelImageForDevice ? FWI_ERR_NODEVICE : FWI_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = (double *)p;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return FWI_ERR_NODEVICE;
     }
-    *out = g_scratch_addr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return e == cudaErrorNoKernelImageForDevice ? FWI_ERR_NODEVICE : FWI_ERR_CUDA;
+    }
+    *out = (double *)p;
     return FWI_OK;
 }
 
@@ -88,8 +87,8 @@ extern "C" int fwi_residual_misfit_noalloc(float *res, const float *syn, const f
                                            void *stream)
 {
     if (!res || !syn || !obs || !misfit || nt <= 0 || nrec <= 0) return FWI_ERR_ARG;
+    if (nt > FWI_NOALLOC_MAX_ELEMENTS / nrec) return FWI_ERR_ARG;  // before nt * nrec can overflow
     const long n = nt * (long)nrec;
-    if (n > FWI_NOALLOC_MAX_ELEMENTS) return FWI_ERR_ARG;
     double *scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc != FWI_OK) return rc;

@@ -62,9 +62,16 @@ class Workload:
         return ((vp * (1 + 2 * e)).astype(np.float32), vp, (vp * (1 + 2 * d)).astype(np.float32))
 
     def point_updates(self, shots=None):
-        """Forward + adjoint point updates of a gradient over `shots` (windows and nt per shot)."""
+        """Forward + adjoint point updates of a gradient over `shots` (windows and nt per shot),
+        counting every grid point of each shot's window, the 4-point frame included."""
         sh = self.shots if shots is None else shots
         return sum(2 * (s["nxw"] or self.nx) * self.nz * s["nt"] for s in sh)
+
+    def physical_point_updates(self, shots=None):
+        """The same over the points a step updates: each window without its 4-point frame
+        (601 x 301 per shot and step for C2, not 609 x 309)."""
+        sh = self.shots if shots is None else shots
+        return sum(2 * ((s["nxw"] or self.nx) - 2 * FRAME) * (self.nz - 2 * FRAME) * s["nt"] for s in sh)
 
     def cfl(self):
         vmax = float((self.vel * np.sqrt(1 + 2 * np.maximum(self.eps, self.delta))).max())

@@ -311,9 +311,11 @@ int fwi_graph_stats(void *ctx, long *out2);
  * Scratch is a fixed array inside the library (FWI_NOALLOC_MAX_BLOCKS + 1 doubles per
  * device, held until the process exits); it limits nt * nrec to FWI_NOALLOC_MAX_ELEMENTS
  * (larger requests return FWI_ERR_ARG).  Every call shares that array, so calls that
- * overlap on the GPU (other streams, other threads) race; serialise them.  The first call
- * on a device looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture. */
+ * overlap on the GPU (other streams, other threads) race; serialise them.  Each call looks
+ * up the array's device address on the current device (cudaGetSymbolAddress); the first
+ * call on a device also loads the library's module there, so make it before any stream
+ * capture.  The mask is ONE row of nrec bytes applied to every one of the nt trace rows
+ * (fwi_misfit takes one row per shot, concatenated): pass a block of shots that share it. */
 #define FWI_NOALLOC_MAX_BLOCKS 16384
 #define FWI_NOALLOC_MAX_ELEMENTS (16384L * 4096L)
 int fwi_residual_misfit_noalloc(float *res, const float *syn, const float *obs,

@@ -67,8 +67,11 @@ def smooth(a, passes=6):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", default=os.environ.get("FWI_REFERENCE_ROOT"),
+                    help="the reference checkout (default: $FWI_REFERENCE_ROOT)")
     args = ap.parse_args()
+    if not args.ref_root:
+        ap.error("give --ref-root or set FWI_REFERENCE_ROOT to the reference checkout")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref",
                     f"REF_ROOT={args.ref_root}"], check=True)
     ref = po.ref_lib()

@@ -240,70 +240,13 @@ def test_single_step_kernels_against_oracle(L):
     assert L.fwi_compat_last_error() == 0
 
 
-def _blocking_stream():
-    for name in ("libcudart.so", "/usr/local/cuda/lib64/libcudart.so"):
-        try:
-            rt = C.CDLL(name)
-            s = C.c_void_p()
-            if rt.cudaStreamCreate(C.byref(s)) == 0:
-                return rt, s.value
-        except OSError:
-            continue
-    return None, 0
-
-
 def test_one_shot_through_launch_functions_matches_reference(L):
     """src/main.c:408-495 for shot 0 of the fixtures, through launchPropagation /
     res_h / launchBackPropagation with the reference's buffer layout and aliasing."""
-    rt, s1 = _blocking_stream()
-    _, s2 = _blocking_stream()
-    n = NX * NZ
-    sx = int(G["shots_sx"][0])
-    dh2 = np.float32(DH * DH)
-    C_ = float(np.float32(np.float32(DT * DT) / dh2))
-    a_x, b_x, a_z, b_z = (dev(G[k]) for k in ("ax", "bx", "az", "bz"))
-    v_hor, v_po, v_nmo = dev(G["vh_i"]), dev(G["vp_i"]), dev(G["vn_i"])
-    source = dev(G["source"])
-    lvlA, lvlB, pre2 = zeros(2 * n), zeros(2 * n), zeros(2 * n)
-    PF, p2, r2 = zeros(n), zeros(n), zeros(n)
-    psi_px, psi_fz, z_px, z_fz, aten_p, aten_f = (zeros(n) for _ in range(6))
-    shot1 = dev(G["obs"][0])
-    shot2, Res = zeros(NT * NX), zeros(NT * NX)
-    PF_h = torch.zeros(NT * 2 * n, dtype=torch.float32).pin_memory()
-    f4 = 4
-
-    P_pre, P_past = lvlA, lvlB
-    for it in range(NT):
-        L.launchPropagation(s1, s2, PF_h.data_ptr() + 2 * it * n * f4, P(PF), P(P_past), P(P_pre),
-                            P(P_past) + n * f4, P(P_pre) + n * f4, P(p2), P(r2), float(dh2), NX, NZ,
-                            P(a_x), P(b_x), P(a_z), P(b_z), P(psi_px), P(psi_fz), DH, CPML, P(z_px),
-                            P(z_fz), P(aten_p), P(aten_f), P(v_hor), P(v_po), P(v_nmo), P(source),
-                            P(shot2), C_, sx, SZ, it)
-        P_pre, P_past = P_past, P_pre
-    L.res_h(P(Res), P(shot1), P(shot2), NX, NT)
-    res = host(Res).reshape(NT, NX)
+    from compat_shot import compat_gradient_shot
+    res, _, g = compat_gradient_shot(L, NX, NZ, NT, CPML, DH, DT, G["ax"], G["bx"], G["az"], G["bz"], G["vh_i"],
+                                     G["vp_i"], G["vn_i"], G["source"], int(G["shots_sx"][0]), SZ, G["obs"][0])
     assert rel_l2(res, G["res"][0]) <= 1e-5
-
-    # adjoint: the reference aliases its forward CPML buffers (src/main.c:184-193)
-    for t in (lvlA, lvlB, psi_px, psi_fz, z_px, z_fz, aten_p, aten_f):
-        t.zero_()
-    psixcx, psixcz, atenxcx, atenxcz, atenzdx, atenzcz = (zeros(n) for _ in range(6))
-    aux = [zeros(n) for _ in range(4)]
-    p2c = [zeros(n) for _ in range(4)]
-    g = [zeros(n) for _ in range(3)]
-    P_pre, P_past = lvlA, lvlB
-    for it in range(NT):
-        L.launchBackPropagation(s1, s2, NX, NZ, NT, PF_h.data_ptr() + (NT - it - 1) * n * 2 * f4, P(P_pre),
-                                P(P_past), P(P_pre) + n * f4, P(P_past) + n * f4, *[P(a) for a in aux],
-                                P(v_hor), P(v_po), P(v_nmo), *[P(a) for a in p2c], float(dh2), P(pre2),
-                                P(pre2) + n * f4, P(a_x), P(b_x), P(a_z), P(b_z), P(psixcx), P(psixcz),
-                                P(psi_px), P(psi_fz), DH, CPML, P(z_px), P(z_fz), P(aten_f), P(aten_p),
-                                P(atenxcx), P(atenxcz), P(atenzdx), P(atenzcz), P(Res), C_, P(PF), it, sx,
-                                SZ, DT, P(g[0]), P(g[1]), P(g[2]))
-        P_pre, P_past = P_past, P_pre
     assert L.fwi_compat_last_error() == 0
     for t, k in zip(g, ("gcx_shot0", "gcz_shot0", "gdx_shot0")):
-        assert rel_l2(host(t).reshape(NZ, NX), G[k]) <= 1e-4, k
-    if rt is not None:
-        rt.cudaStreamDestroy(C.c_void_p(s1))
-        rt.cudaStreamDestroy(C.c_void_p(s2))
+        assert rel_l2(t, G[k]) <= 1e-4, k

@@ -2,8 +2,8 @@
 unchanged as C99 against its own headers (with a one-rank MPI stand-in,
 tests/mpi_stub/mpi.h, for the MPI it uses), links against libfwi_gb300.so
 and the CUDA runtime with no symbol left unresolved; the library replaces
-the reference's two CUDA objects.  Needs the reference checkout (default
-/root/reference, or FWI_REFERENCE_ROOT); skipped where it is absent."""
+the reference's two CUDA objects.  Needs the reference checkout, named by
+the environment variable FWI_REFERENCE_ROOT; skipped where it is not given."""
 import os
 import shutil
 import subprocess
@@ -11,15 +11,15 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("FWI_REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("FWI_REFERENCE_ROOT", "")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
 def test_reference_main_links_against_the_library(tmp_path):
-    main_c = os.path.join(REF, "src", "main.c")
+    main_c = os.path.join(REF, "src", "main.c") if REF else ""
     cudart = os.path.join(CUDA, "lib64")
     gcc = shutil.which("gcc")
-    if not os.path.exists(main_c) or gcc is None or not os.path.exists(os.path.join(CUDA, "include", "cuda_runtime.h")):
+    if not main_c or not os.path.exists(main_c) or gcc is None or not os.path.exists(os.path.join(CUDA, "include", "cuda_runtime.h")):
         pytest.skip("needs the reference checkout, gcc and the CUDA toolkit")
     from fwi_gb300 import build
     libdir = os.path.dirname(build.build())

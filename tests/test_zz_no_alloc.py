@@ -7,7 +7,6 @@ the FP64 summation-order tolerance, call after call.
 
 Collected last (file name) so that a run stopping at the first failure has
 already run every other test."""
-import ctypes as C
 import os
 
 import numpy as np
@@ -17,6 +16,11 @@ pytestmark = pytest.mark.gpu
 
 G = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_small.npz"))
 NX, NZ, NT, CPML, SZ = (int(G[k]) for k in ("nx", "nz", "nt", "cpml", "sz"))
+
+
+def call(L, res, syn, obs, mask, nt, nrec, mis):
+    return L.fwi_residual_misfit_noalloc(res.data_ptr(), syn.data_ptr(), obs.data_ptr(),
+                                         None if mask is None else mask.data_ptr(), nt, nrec, mis.data_ptr(), None)
 
 
 def test_noalloc_misfit_matches_context_path_twice():
@@ -34,6 +38,7 @@ def test_noalloc_misfit_matches_context_path_twice():
     mask = np.ones(2 * nrec, np.uint8)
     mask[5::11] = 0
     J_ctx = ctx.misfit(shots, obs, mask)
+    J_ctx_nomask = ctx.misfit(shots, obs, None)
 
     syn = torch.zeros(2 * NT * nrec, dtype=torch.float32, device="cuda")
     ctx.forward(shots, out=syn)
@@ -44,18 +49,61 @@ def test_noalloc_misfit_matches_context_path_twice():
     res = torch.full_like(syn, float("nan"))
     mis = torch.zeros(1, dtype=torch.float64, device="cuda")
     want_res = ((syn - obs_d).view(2 * NT, nrec) * mask_d.to(torch.float32)).view(-1)
-    for call in range(2):
-        rc = L.fwi_residual_misfit_noalloc(res.data_ptr(), syn.data_ptr(), obs_d.data_ptr(),
-                                           mask_d.data_ptr(), 2 * NT, nrec, mis.data_ptr(), None)
-        assert rc == 0
+    for rep in range(2):
+        assert call(L, res, syn, obs_d, mask_d, 2 * NT, nrec, mis) == 0
         torch.cuda.synchronize()
         J = float(mis.item())
-        assert abs(J - J_ctx) <= 1e-12 * J_ctx, (call, J, J_ctx)
+        assert abs(J - J_ctx) <= 1e-12 * J_ctx, (rep, J, J_ctx)
         assert torch.equal(res, want_res)
         res.fill_(float("nan"))
         mis.zero_()
 
-    # a request beyond the scratch array's limit is refused before any launch
-    big = int(L.fwi_residual_misfit_noalloc(res.data_ptr(), syn.data_ptr(), obs_d.data_ptr(), None,
-                                            (16384 * 4096) // nrec + 1, nrec, mis.data_ptr(), None))
+    # no mask: every trace counts, against the context path and an FP64 sum here
+    d64 = (syn.double() - obs_d.double())
+    want_nomask = 0.5 * float((d64 * d64).sum())
+    assert call(L, res, syn, obs_d, None, 2 * NT, nrec, mis) == 0
+    torch.cuda.synchronize()
+    J = float(mis.item())
+    assert abs(J - J_ctx_nomask) <= 1e-12 * J_ctx_nomask
+    assert abs(J - want_nomask) <= 1e-12 * want_nomask
+    assert torch.equal(res, syn - obs_d)
+
+    # a request beyond the scratch array's limit is refused before any launch, also when
+    # nt * nrec would not fit in a long
+    big = call(L, res, syn, obs_d, None, (16384 * 4096) // nrec + 1, nrec, mis)
     assert big == native.FWI_ERR_ARG
+    assert call(L, res, syn, obs_d, None, 2 ** 62, nrec, mis) == native.FWI_ERR_ARG
+
+
+def test_noalloc_partial_blocks_and_changing_sizes_repeat_exactly():
+    """Sizes that are not a multiple of one block's 4096 samples and span several
+    blocks, alternated, repeat bit for bit: every call starts its completion
+    counter from zero, whatever size the call before it had."""
+    torch = pytest.importorskip("torch")
+    from fwi_gb300 import native
+    L = native.lib()
+    g = torch.Generator(device="cuda").manual_seed(7)
+    for nt, nrec in ((37, 301), (5, 17), (1031, 77), (37, 301), (5, 17), (1031, 77)):
+        n = nt * nrec
+        syn = torch.randn(n, generator=g, device="cuda")
+        obs = torch.randn(n, generator=g, device="cuda")
+        res = torch.empty_like(syn)
+        mis = torch.zeros(1, dtype=torch.float64, device="cuda")
+        assert call(L, res, syn, obs, None, nt, nrec, mis) == 0
+        torch.cuda.synchronize()
+        d = syn.double() - obs.double()
+        want = 0.5 * float((d * d).sum())
+        J = float(mis.item())
+        assert abs(J - want) <= 1e-12 * want, (nt, nrec, J, want)
+        assert torch.equal(res, syn - obs)
+    # the same inputs twice in a row give the same bits
+    syn = torch.randn(1031 * 77, generator=g, device="cuda")
+    obs = torch.randn(1031 * 77, generator=g, device="cuda")
+    res = torch.empty_like(syn)
+    mis = torch.zeros(1, dtype=torch.float64, device="cuda")
+    got = []
+    for _ in range(2):
+        assert call(L, res, syn, obs, None, 1031, 77, mis) == 0
+        torch.cuda.synchronize()
+        got.append(float(mis.item()))
+    assert got[0] == got[1]
