@@ -2,8 +2,14 @@
 // entry points (include/serialcalls.h) on the library's own sm_103a kernels.
 //
 // Buffer semantics are the reference's: every array the reference kernels
-// write is written here, with the same values up to FP32 rounding, and
-// nothing else is touched.  The per-step sequences of the reference
+// write is written here, and nothing else is touched.  The arithmetic is the
+// reference's too, operation for operation: stencil differences and pair sums
+// in FP32, the double-literal coefficients and the division by dh (dh2) in
+// FP64, rounding to FP32 on assignment, everything else in FP32 in the
+// reference's operand order.  This unit is compiled without multiply-add
+// contraction (--fmad=false, fwi_gb300/build.py), so every operation rounds
+// as C evaluates the expression, and the results equal the reference kernels
+// run as C on the CPU bit for bit.  The per-step sequences of the reference
 // (launchPropagation: 4 kernels; launchBackPropagation: 6 kernels) run as 2
 // and 3 kernels: one pass over the CPML strip points (the memory variables
 // whose derivatives the next pass needs), then one tiled pass that stages
@@ -34,6 +40,40 @@ inline void note(cudaError_t e)
 inline void note_launch() { note(cudaGetLastError()); }
 
 inline dim3 tile_grid(int nx, int nz) { return dim3((nx + TX - 1) / TX, (nz + TZ - 1) / TZ); }
+
+// The reference's 8th-order stencils (src/parallelcalls.cu:57, 127).  v(k) is the
+// FP32 value k points from the centre along the stencil's axis.  Differences and
+// pair sums of neighbours are FP32 operations; the coefficients are double
+// literals, so the products, the sum and the division by dh (dh2) are FP64; the
+// caller rounds the result to FP32.
+template <typename V> __device__ __forceinline__ double ref_first(V v, float dh)
+{
+    return ((4 / 5.) * (v(1) - v(-1)) - (1 / 5.) * (v(2) - v(-2)) + (4 / 105.) * (v(3) - v(-3)) -
+            (1 / 280.) * (v(4) - v(-4))) /
+           dh;
+}
+
+template <typename V> __device__ __forceinline__ double ref_second(V v, float dh2)
+{
+    return (-(205 / 72.) * v(0) + (8 / 5.) * (v(1) + v(-1)) - (1 / 5.) * (v(2) + v(-2)) +
+            (8 / 315.) * (v(3) + v(-3)) - (1 / 560.) * (v(4) + v(-4))) /
+           dh2;
+}
+
+// Along x (s = 1) or z (s = nx) of a global array, at flat index i.
+__device__ __forceinline__ float first_g(const float *f, long i, long s, float dh)
+{
+    return (float)ref_first([&](int k) { return f[i + k * s]; }, dh);
+}
+// From a staged x-halo tile [rows][W] (output column c, row r) or z-halo tile [rows + 8][TX].
+template <int W> __device__ __forceinline__ float second_xt(const float (*t)[W], int r, int c, float dh2)
+{
+    return (float)ref_second([&](int k) { return t[r][c + fwi::kRad + k]; }, dh2);
+}
+__device__ __forceinline__ float second_zt(const float (*t)[TX], int r, int c, float dh2)
+{
+    return (float)ref_second([&](int k) { return t[r + fwi::kRad + k][c]; }, dh2);
+}
 inline unsigned blocks1d(long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 // ----------------------------------------------------------------- setup
@@ -87,7 +127,7 @@ __global__ void k_cpml_z(float *a_z, float *b_z, int cpml, float vmax, int nz, f
 __global__ void k_psi_f_strip(const float *__restrict__ P, const float *__restrict__ F,
                               const float *__restrict__ a_x, const float *__restrict__ b_x,
                               const float *__restrict__ a_z, const float *__restrict__ b_z,
-                              float *psi_px, float *psi_fz, StripMap sm, float inv_dh)
+                              float *psi_px, float *psi_fz, StripMap sm, float dh)
 {
     const int nx = sm.nx;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < sm.count();
@@ -95,8 +135,8 @@ __global__ void k_psi_f_strip(const float *__restrict__ P, const float *__restri
         int ix, iz;
         sm.point(k, ix, iz);
         long i = (long)iz * nx + ix;
-        float tpx = fwi::d1_strided(P, i, 1) * inv_dh;
-        float tfz = fwi::d1_strided(F, i, nx) * inv_dh;
+        float tpx = first_g(P, i, 1, dh);
+        float tfz = first_g(F, i, nx, dh);
         psi_px[i] = b_x[ix] * psi_px[i] + a_x[ix] * tpx;
         psi_fz[i] = b_z[iz] * psi_fz[i] + a_z[iz] * tfz;
     }
@@ -107,7 +147,7 @@ __global__ void k_zeta_f_strip(const float *__restrict__ p2, const float *__rest
                                const float *__restrict__ a_z, const float *__restrict__ b_z,
                                const float *__restrict__ psi_px, const float *__restrict__ psi_fz,
                                float *z_px, float *z_fz, float *aten_p, float *aten_f, StripMap sm,
-                               float inv_dh)
+                               float dh)
 {
     const int nx = sm.nx;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < sm.count();
@@ -115,8 +155,8 @@ __global__ void k_zeta_f_strip(const float *__restrict__ p2, const float *__rest
         int ix, iz;
         sm.point(k, ix, iz);
         long i = (long)iz * nx + ix;
-        float tx = fwi::d1_strided(psi_px, i, 1) * inv_dh;
-        float tz = fwi::d1_strided(psi_fz, i, nx) * inv_dh;
+        float tx = first_g(psi_px, i, 1, dh);
+        float tz = first_g(psi_fz, i, nx, dh);
         float zp = b_x[ix] * z_px[i] + a_x[ix] * (p2[i] + tx);
         float zf = b_z[iz] * z_fz[i] + a_z[iz] * (r2[i] + tz);
         z_px[i] = zp;
@@ -127,7 +167,7 @@ __global__ void k_zeta_f_strip(const float *__restrict__ p2, const float *__rest
 }
 
 __global__ void k_second_p(const float *__restrict__ P, const float *__restrict__ F, float *p2,
-                           float *r2, float inv_dh2, int nx, int nz)
+                           float *r2, float dh2, int nx, int nz)
 {
     __shared__ float sP[TZ][XW];
     __shared__ float sF[ZH][TX];
@@ -140,8 +180,8 @@ __global__ void k_second_p(const float *__restrict__ P, const float *__restrict_
         int iz = z0 + r;
         if (!interior(ix, iz, nx, nz)) continue;
         long i = (long)iz * nx + ix;
-        p2[i] = fwi::d2x_tile<float, XW>(sP, r, c) * inv_dh2;
-        r2[i] = fwi::d2z_tile<float, TX>(sF, r, c) * inv_dh2;
+        p2[i] = second_xt<XW>(sP, r, c, dh2);
+        r2[i] = second_zt(sF, r, c, dh2);
     }
 }
 
@@ -210,8 +250,8 @@ k_fwd_main(float *p2, float *r2, float *PF, const float *__restrict__ P_pre,
            const float *__restrict__ psi_px, const float *__restrict__ psi_fz, float *z_px,
            float *z_fz, float *aten_p, float *aten_f, const float *__restrict__ v_hor,
            const float *__restrict__ v_po, const float *__restrict__ v_nmo,
-           const float *__restrict__ source, float *shot, float C, float dh2, float inv_dh,
-           float inv_dh2, int nx, int nz, int sx, int sz, int it, int cpml)
+           const float *__restrict__ source, float *shot, float C, float dh2, float dh, int nx, int nz,
+           int sx, int sz, int it, int cpml)
 {
     __shared__ float sP[TZ][XW];
     __shared__ float sF[ZH][TX];
@@ -227,13 +267,13 @@ k_fwd_main(float *p2, float *r2, float *PF, const float *__restrict__ P_pre,
         const long i = (long)iz * nx + ix;
         float p2v = 0.f, r2v = 0.f, atp = 0.f, atf = 0.f;
         if (interior(ix, iz, nx, nz)) {
-            p2v = fwi::d2x_tile<float, XW>(sP, r, c) * inv_dh2;
-            r2v = fwi::d2z_tile<float, TX>(sF, r, c) * inv_dh2;
+            p2v = second_xt<XW>(sP, r, c, dh2);
+            r2v = second_zt(sF, r, c, dh2);
             p2[i] = p2v;
             r2[i] = r2v;
             if (in_strip(ix, iz, nx, nz, cpml)) {
-                float tx = fwi::d1_strided(psi_px, i, 1) * inv_dh;
-                float tz = fwi::d1_strided(psi_fz, i, nx) * inv_dh;
+                float tx = first_g(psi_px, i, 1, dh);
+                float tz = first_g(psi_fz, i, nx, dh);
                 float zp = b_x[ix] * z_px[i] + a_x[ix] * (p2v + tx);
                 float zf = b_z[iz] * z_fz[i] + a_z[iz] * (r2v + tz);
                 z_px[i] = zp;
@@ -273,7 +313,7 @@ __global__ void k_psi_r_strip(const float *__restrict__ aux1, const float *__res
                               const float *__restrict__ a_x, const float *__restrict__ b_x,
                               const float *__restrict__ a_z, const float *__restrict__ b_z,
                               float *psixcx, float *psixcz, float *psizdx, float *psizcz,
-                              StripMap sm, float inv_dh)
+                              StripMap sm, float dh)
 {
     const int nx = sm.nx;
     for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < sm.count();
@@ -281,10 +321,10 @@ __global__ void k_psi_r_strip(const float *__restrict__ aux1, const float *__res
         int ix, iz;
         sm.point(k, ix, iz);
         long i = (long)iz * nx + ix;
-        float p1cx = fwi::d1_strided(aux1, i, 1) * inv_dh;
-        float p1cz = fwi::d1_strided(aux2, i, nx) * inv_dh;
-        float r1dx = fwi::d1_strided(aux3, i, 1) * inv_dh;
-        float r1cz = fwi::d1_strided(aux4, i, nx) * inv_dh;
+        float p1cx = first_g(aux1, i, 1, dh);
+        float p1cz = first_g(aux2, i, nx, dh);
+        float r1dx = first_g(aux3, i, 1, dh);
+        float r1cz = first_g(aux4, i, nx, dh);
         psixcx[i] = b_x[ix] * psixcx[i] + a_x[ix] * p1cx;
         psixcz[i] = b_z[iz] * psixcz[i] + a_z[iz] * p1cz;
         psizdx[i] = b_x[ix] * psizdx[i] + a_x[ix] * r1dx;
@@ -304,7 +344,7 @@ struct AdjArgs {
     const float *Res;
     const float *P_snap, *F_snap;
     float *gcx, *gcz, *gdx;
-    float C, dh2, dt, inv_dh, inv_dh2;
+    float C, dh2, dt, dh;
     int nx, nz, nt, sz, it, cpml;
 };
 
@@ -336,20 +376,20 @@ __global__ void __launch_bounds__(TX * BY) k_adj_main(AdjArgs a)
         const bool upd = interior(ix, iz, nx, nz);
         float pn = 0.f, fn = 0.f;
         if (upd) {
-            float p2cx = fwi::d2x_tile<float, XW>(s1, r, c) * a.inv_dh2;
-            float r2dx = fwi::d2x_tile<float, XW>(s3, r, c) * a.inv_dh2;
-            float p2cz = fwi::d2z_tile<float, TX>(s2, r, c) * a.inv_dh2;
-            float r2cz = fwi::d2z_tile<float, TX>(s4, r, c) * a.inv_dh2;
+            float p2cx = second_xt<XW>(s1, r, c, a.dh2);
+            float r2dx = second_xt<XW>(s3, r, c, a.dh2);
+            float p2cz = second_zt(s2, r, c, a.dh2);
+            float r2cz = second_zt(s4, r, c, a.dh2);
             a.p2cx[i] = p2cx;
             a.r2dx[i] = r2dx;
             a.p2cz[i] = p2cz;
             a.r2cz[i] = r2cz;
             float axcx, axcz, azdx, azcz;
             if (in_strip(ix, iz, nx, nz, a.cpml)) {
-                float dxcx = fwi::d1_strided(a.psixcx, i, 1) * a.inv_dh;
-                float dxcz = fwi::d1_strided(a.psixcz, i, nx) * a.inv_dh;
-                float dzdx = fwi::d1_strided(a.psizdx, i, 1) * a.inv_dh;
-                float dzcz = fwi::d1_strided(a.psizcz, i, nx) * a.inv_dh;
+                float dxcx = first_g(a.psixcx, i, 1, a.dh);
+                float dxcz = first_g(a.psixcz, i, nx, a.dh);
+                float dzdx = first_g(a.psizdx, i, 1, a.dh);
+                float dzcz = first_g(a.psizcz, i, nx, a.dh);
                 float bx = a.b_x[ix], ax = a.a_x[ix], bz = a.b_z[iz], az = a.a_z[iz];
                 float zxcx = bx * a.zitaxcx[i] + ax * (dxcx + p2cx);
                 float zxcz = bz * a.zitaxcz[i] + az * (dxcz + p2cz);
@@ -382,8 +422,8 @@ __global__ void __launch_bounds__(TX * BY) k_adj_main(AdjArgs a)
         if (inj) { float d = res_row[ix]; pn += d; fn += d; }
         if (upd || inj) { a.P_past[i] = pn; a.F_past[i] = fn; }
         if (upd) {
-            float p2 = fwi::d2x_tile<float, XW>(sS, r, c) * a.inv_dh2;
-            float r2 = fwi::d2z_tile<float, TX>(sT, r, c) * a.inv_dh2;
+            float p2 = second_xt<XW>(sS, r, c, a.dh2);
+            float r2 = second_zt(sT, r, c, a.dh2);
             a.gcx[i] += a.dt * p2 * pn;
             a.gcz[i] += a.dt * r2 * (pn + fn);
             a.gdx[i] += a.dt * p2 * fn;
@@ -553,7 +593,7 @@ void PSI_F_h(float *P, float *F, float *a_x, float *b_x, float *a_z, float *b_z,
     StripMap sm = StripMap::make(nx, nz, CPML);
     if (sm.count() == 0) return;
     k_psi_f_strip<<<elt_grid(sm.count()), kEltBlock>>>(P, F, a_x, b_x, a_z, b_z, psi_px, psi_fz,
-                                                         sm, 1.0f / dh);
+                                                         sm, dh);
     note_launch();
 }
 
@@ -566,7 +606,7 @@ void ZETA_F_h(float *p2, float *r2, float *P, float *F, float *a_x, float *b_x, 
     if (sm.count() == 0) return;
     k_zeta_f_strip<<<elt_grid(sm.count()), kEltBlock>>>(p2, r2, a_x, b_x, a_z, b_z, psi_px,
                                                           psi_fz, z_px, z_fz, aten_p, aten_f, sm,
-                                                          1.0f / dh);
+                                                          dh);
     note_launch();
 }
 
@@ -591,7 +631,7 @@ void res_h(float *Res, float *shot1, float *shot2, int nx, int nz)
 void SecondDerivate_P_h(float *P_pre, float *F_pre, float *p2, float *r2, float dh2, int nx,
                         int nz)
 {
-    k_second_p<<<tile_grid(nx, nz), dim3(TX, BY)>>>(P_pre, F_pre, p2, r2, 1.0f / dh2, nx, nz);
+    k_second_p<<<tile_grid(nx, nz), dim3(TX, BY)>>>(P_pre, F_pre, p2, r2, dh2, nx, nz);
     note_launch();
 }
 
@@ -608,12 +648,11 @@ void launchPropagation(cudaStream_t stream1, cudaStream_t stream2, float *PF_h, 
     StripMap sm = StripMap::make(nx, nz, CPML);
     if (sm.count() > 0)
         k_psi_f_strip<<<elt_grid(sm.count()), kEltBlock, 0, stream2>>>(
-            P_pre, F_pre, a_x, b_x, a_z, b_z, psi_px, psi_fz, sm, 1.0f / dh);
+            P_pre, F_pre, a_x, b_x, a_z, b_z, psi_px, psi_fz, sm, dh);
     // legacy default stream: waits for the copy on stream1 and the strip pass on stream2
     k_fwd_main<<<tile_grid(nx, nz), dim3(TX, BY), 0, cudaStreamLegacy>>>(
         p2, r2, PF, P_pre, F_pre, P_past, F_past, a_x, b_x, a_z, b_z, psi_px, psi_fz, z_px, z_fz,
-        aten_p, aten_f, v_hor, v_po, v_nmo, source, shot2, C, dh2, 1.0f / dh, 1.0f / dh2, nx, nz,
-        sx, sz, it, CPML);
+        aten_p, aten_f, v_hor, v_po, v_nmo, source, shot2, C, dh2, dh, nx, nz, sx, sz, it, CPML);
     note_launch();
 }
 
@@ -639,8 +678,7 @@ void launchBackPropagation(cudaStream_t stream1, cudaStream_t stream2, int nx, i
     StripMap sm = StripMap::make(nx, nz, CPML);
     if (sm.count() > 0)
         k_psi_r_strip<<<elt_grid(sm.count()), kEltBlock, 0, stream2>>>(
-            aux1, aux2, aux3, aux4, a_x, b_x, a_z, b_z, psixcx, psixcz, psizdx, psizcz, sm,
-            1.0f / dh);
+            aux1, aux2, aux3, aux4, a_x, b_x, a_z, b_z, psixcx, psixcz, psizdx, psizcz, sm, dh);
     AdjArgs a;
     a.aux1 = aux1; a.aux2 = aux2; a.aux3 = aux3; a.aux4 = aux4;
     a.p2cx = p2cx; a.p2cz = p2cz; a.r2dx = r2dx; a.r2cz = r2cz;
@@ -651,7 +689,7 @@ void launchBackPropagation(cudaStream_t stream1, cudaStream_t stream2, int nx, i
     a.P_pre = P_pre; a.F_pre = F_pre; a.P_past = P_past; a.F_past = F_past;
     a.Res = Res; a.P_snap = P_pre2; a.F_snap = F_pre2;
     a.gcx = gcx; a.gcz = gcz; a.gdx = gdx;
-    a.C = C; a.dh2 = dh2; a.dt = dt; a.inv_dh = 1.0f / dh; a.inv_dh2 = 1.0f / dh2;
+    a.C = C; a.dh2 = dh2; a.dt = dt; a.dh = dh;
     a.nx = nx; a.nz = nz; a.nt = nt; a.sz = sz; a.it = it; a.cpml = CPML;
     // legacy default stream: after the H2D copy (stream1) and the strip pass (stream2)
     k_adj_main<<<tile_grid(nx, nz), dim3(TX, BY), 0, cudaStreamLegacy>>>(a);

@@ -58,8 +58,9 @@ def test_noalloc_misfit_matches_context_path_twice():
         res.fill_(float("nan"))
         mis.zero_()
 
-    # no mask: every trace counts, against the context path and an FP64 sum here
-    d64 = (syn.double() - obs_d.double())
+    # no mask: every trace counts, against the context path and an FP64 sum here of the
+    # FP32 differences (the residual is an FP32 array; its squares accumulate in FP64)
+    d64 = (syn - obs_d).double()
     want_nomask = 0.5 * float((d64 * d64).sum())
     assert call(L, res, syn, obs_d, None, 2 * NT, nrec, mis) == 0
     torch.cuda.synchronize()
@@ -91,7 +92,7 @@ def test_noalloc_partial_blocks_and_changing_sizes_repeat_exactly():
         mis = torch.zeros(1, dtype=torch.float64, device="cuda")
         assert call(L, res, syn, obs, None, nt, nrec, mis) == 0
         torch.cuda.synchronize()
-        d = syn.double() - obs.double()
+        d = (syn - obs).double()
         want = 0.5 * float((d * d).sum())
         J = float(mis.item())
         assert abs(J - want) <= 1e-12 * want, (nt, nrec, J, want)
