@@ -449,22 +449,28 @@ def accuracy(args, w, context, obs_d, fwi_gb300):
 
 def inversion(args, w, context, obs_d, shots, torch):
     """The workload's inversion loop through the C driver (fwi_invert: steepest first step, then L-BFGS
-    with the backtracking line search, src/main.c:396-801) from the initial model, timed end to end."""
-    ctx = context(min(args.batch, len(w.shots)))
-    ctx.set_model(*w.squared(initial=True))
-    if args.autotune > 0:
-        ctx.autotune(shots, steps=args.autotune)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    hist = ctx.invert(shots, obs_d, w.mask, iterations=args.invert_iters, lbfgs_m=5)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    del ctx
-    return {"iterations": len(hist), "requested": args.invert_iters, "lbfgs_m": 5, "storage": args.storage,
-            "wall_s": round(dt, 3), "s_per_iteration": round(dt / max(1, len(hist)), 4),
-            "misfit_first": float(hist[0]) if len(hist) else None,
-            "misfit_last": float(hist[-1]) if len(hist) else None,
-            "misfit_history": [float(x) for x in hist]}
+    with the backtracking line search, src/main.c:396-801) from the initial model, timed end to end:
+    the reference's policy as it is, and with the curvature safeguard (pairs with y.s <= 0 skipped)
+    and the step length reset to 1 at each iteration."""
+    out = {}
+    for name, opts in (("reference_policy", {}), ("curvature_guard", {"curvature_guard": 1, "reset_alpha": 1})):
+        ctx = context(min(args.batch, len(w.shots)))
+        ctx.set_model(*w.squared(initial=True))
+        if args.autotune > 0:
+            ctx.autotune(shots, steps=args.autotune)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist = ctx.invert(shots, obs_d, w.mask, iterations=args.invert_iters, lbfgs_m=5, **opts)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        del ctx
+        out[name] = {"options": opts, "iterations": len(hist), "requested": args.invert_iters, "lbfgs_m": 5,
+                     "storage": args.storage, "wall_s": round(dt, 3),
+                     "s_per_iteration": round(dt / max(1, len(hist)), 4),
+                     "misfit_first": float(hist[0]) if len(hist) else None,
+                     "misfit_last": float(hist[-1]) if len(hist) else None,
+                     "misfit_history": [round(float(x), 3) for x in hist]}
+    return out
 
 
 def reference_arm(args, rank, world, dist):

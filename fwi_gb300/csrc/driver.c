@@ -41,6 +41,7 @@ void fwi_invert_defaults(fwi_invert_opts *o)
     o->flag_min = 0;            /* src/main.c:693 passes 0, 0 */
     o->flag_max = 0;
     o->armijo_c1 = 0.0;
+    o->curvature_guard = 0;     /* the reference's two-loop: every pair */
 }
 
 int fwi_invert(void *ctx, const fwi_shot *shots, int nshots, const void *obs, const unsigned char *mask,
@@ -53,7 +54,8 @@ int fwi_invert(void *ctx, const fwi_shot *shots, int nshots, const void *obs, co
     float alpha = o.alpha0;
     int count = 0;
     int done = 0;
-    int rc = FWI_OK;
+    int rc = fwi_set_lbfgs_guard(ctx, o.curvature_guard);
+    if (rc != FWI_OK) return rc;
     for (int n = 0; n < o.iterations; n++) {
         double phi = 0.0;
         rc = fwi_gradient(ctx, shots, nshots, obs, mask, NULL, NULL, NULL, &phi);

@@ -262,7 +262,7 @@ template <typename T> struct CTri {
     const T *p[3];
 };
 
-// s_k = m - m_back, y_k = g - g_back (3 parameters), and the dots y.s, y.y, s.g.
+// s_k = m - m_back, y_k = g - g_back (3 parameters), and the dots y.s, y.y, s.g, s.s.
 template <typename T>
 __global__ void k_lb_pair(Tri<T> s, Tri<T> y, CTri<T> m, CTri<T> mb, CTri<T> g, CTri<T> gb, long n,
                           DotScratch ds, double *out)
@@ -276,8 +276,9 @@ __global__ void k_lb_pair(Tri<T> s, Tri<T> y, CTri<T> m, CTri<T> mb, CTri<T> g, 
             v[0][p] += (double)yv * sv;
             v[1][p] += (double)yv * yv;
             v[2][p] += (double)sv * g.p[p][i];
+            v[3][p] += (double)sv * sv;
         }
-    reduce_last_block(v, 3, ds, out);
+    reduce_last_block(v, 4, ds, out);
 }
 
 // v := w (copy) and the dots a.w for the first loop's first slot.
@@ -316,34 +317,64 @@ __global__ void k_lb_axpy_dot(Tri<T> x, CTri<T> u, const double *c0, const doubl
 struct LbScalars {
     double rho[3][kMaxHist];
     double alpha[3][kMaxHist];
+    double ys[3][kMaxHist], yy[3][kMaxHist];  // curvature of each slot's pair when it was formed
     double gamma[3];
     double coefA[3], coefB[3];  // scratch coefficients for the next axpy
     double dots[12];
-    double pair[12];            // y.s, y.y, s.g of the newest pair
+    double pair[12];            // y.s, y.y, s.g, s.s of the newest pair
 };
 
-// mode 0: newest pair formed: rho_k = 1/(y.s), first-loop alpha_k = rho_k (s_k.q) with q = g
+// History slots newest .. oldest, for the scaling of the initial matrix.
+struct LbOrder {
+    int n;
+    int slot[kMaxHist];
+};
+
+// mode 0: newest pair formed: rho_k = 1/(y.s), first-loop alpha_k = rho_k (s_k.q) with q = g;
+//         with `guard`, a pair whose y.s <= 0 (no positive curvature along s) gets rho = 0 and so
+//         takes no part in either loop
 // mode 1: alpha_l = rho_l (s_l.q) from dots[0..2]
-// mode 2: gamma = (s.y)/(y.y); coefA = gamma
 // mode 3: beta = rho_l (y_l.r) from dots; coefB = alpha_l - beta
-__global__ void k_lb_scalar(LbScalars *S, int mode, int slot)
+__global__ void k_lb_scalar(LbScalars *S, int mode, int slot, int guard)
 {
     if (threadIdx.x != 0) return;
     for (int p = 0; p < 3; p++) {
         if (mode == 0) {
-            S->rho[p][slot] = 1.0 / S->pair[p];
+            S->ys[p][slot] = S->pair[p];
+            S->yy[p][slot] = S->pair[3 + p];
+            S->rho[p][slot] = (guard && !(S->pair[p] > 0.0)) ? 0.0 : 1.0 / S->pair[p];
             S->alpha[p][slot] = S->rho[p][slot] * S->pair[6 + p];
             S->coefB[p] = -S->alpha[p][slot];
         } else if (mode == 1) {
             S->alpha[p][slot] = S->rho[p][slot] * S->dots[p];
             S->coefB[p] = -S->alpha[p][slot];
-        } else if (mode == 2) {
-            S->gamma[p] = S->pair[p] / S->pair[3 + p];
-            S->coefA[p] = S->gamma[p];
         } else {
             double beta = S->rho[p][slot] * S->dots[p];
             S->coefB[p] = S->alpha[p][slot] - beta;
         }
+    }
+}
+
+// Scaling of the initial matrix, coefA = gamma = (s.y)/(y.y) of the newest pair (src/main.c:622-655).
+// With `guard`: of the newest pair with positive curvature; without one, |s| / |y| of the newest
+// pair (a step as long as the last one, along the gradient).
+__global__ void k_lb_gamma(LbScalars *S, LbOrder o, int guard)
+{
+    if (threadIdx.x != 0) return;
+    for (int p = 0; p < 3; p++) {
+        double gam = S->pair[p] / S->pair[3 + p];
+        if (guard) {
+            gam = sqrt(S->pair[9 + p] / S->pair[3 + p]);
+            for (int a = 0; a < o.n; a++) {
+                const int l = o.slot[a];
+                if (S->ys[p][l] > 0.0) {
+                    gam = S->ys[p][l] / S->yy[p][l];
+                    break;
+                }
+            }
+        }
+        S->gamma[p] = gam;
+        S->coefA[p] = gam;
     }
 }
 
@@ -532,6 +563,7 @@ struct CtxBase {
     virtual int check_bounded_wait(long polls) = 0;
     virtual int first_step(float, float, float) = 0;
     virtual int lbfgs_direction(int, double *) = 0;
+    virtual void set_lbfgs_guard(int) = 0;
     virtual int lbfgs_update(float, float, float, int, int) = 0;
     virtual int direction_slope(double *) = 0;
     virtual int restore_model() = 0;
@@ -727,6 +759,7 @@ template <typename T> struct Ctx : CtxBase {
     bool have_back = false;
     bool have_dir = false;  // r holds an L-BFGS direction from (mb, gb)
     LbScalars *lbs = nullptr;
+    int lb_guard = 0;  // fwi_set_lbfgs_guard: skip pairs without positive curvature
     DotScratch ds{};
     T *vti_out[3] = {};
 
@@ -1804,12 +1837,12 @@ template <typename T> struct Ctx : CtxBase {
         // first loop; q = g and rho_k, alpha_k of the newest pair
         int rcq = copy3(q, grad);
         if (rcq) return rcq;
-        k_lb_scalar<<<1, 32, 0, st>>>(lbs, 0, order[0]);
+        k_lb_scalar<<<1, 32, 0, st>>>(lbs, 0, order[0], lb_guard);
         // rho of the older slots persists from when they were formed
         for (size_t a = 0; a < order.size(); a++) {
             const int l = order[a];
             T *yl[3] = {hy[l][0], hy[l][1], hy[l][2]};
-            if (a > 0) k_lb_scalar<<<1, 32, 0, st>>>(lbs, 1, l);
+            if (a > 0) k_lb_scalar<<<1, 32, 0, st>>>(lbs, 1, l, lb_guard);
             const bool has_next = a + 1 < order.size();
             const int ln = has_next ? order[a + 1] : l;
             T *sn[3] = {hs[ln][0], hs[ln][1], hs[ln][2]};
@@ -1817,7 +1850,10 @@ template <typename T> struct Ctx : CtxBase {
                                                                  has_next ? 1 : 0, mslot, ds, lbs->dots);
         }
         // r = gamma q; then the second loop oldest .. newest
-        k_lb_scalar<<<1, 32, 0, st>>>(lbs, 2, 0);
+        LbOrder lo{};
+        lo.n = (int)order.size();
+        for (int a = 0; a < lo.n; a++) lo.slot[a] = order[a];
+        k_lb_gamma<<<1, 32, 0, st>>>(lbs, lo, lb_guard);
         int first = order.back();
         T *y0[3] = {hy[first][0], hy[first][1], hy[first][2]};
         rcq = copy3(r, q);
@@ -1827,7 +1863,7 @@ template <typename T> struct Ctx : CtxBase {
         for (int a = (int)order.size() - 1; a >= 0; a--) {
             const int l = order[a];
             T *sl[3] = {hs[l][0], hs[l][1], hs[l][2]};
-            k_lb_scalar<<<1, 32, 0, st>>>(lbs, 3, l);
+            k_lb_scalar<<<1, 32, 0, st>>>(lbs, 3, l, lb_guard);
             const bool has_next = a > 0;
             const int ln = has_next ? order[a - 1] : l;
             T *yn[3] = {hy[ln][0], hy[ln][1], hy[ln][2]};
@@ -1852,6 +1888,8 @@ template <typename T> struct Ctx : CtxBase {
         TRY(cudaStreamSynchronize(st));
         return FWI_OK;
     }
+
+    void set_lbfgs_guard(int on) override { lb_guard = on ? 1 : 0; }
 
     int direction_slope(double *out3) override
     {
@@ -2062,6 +2100,13 @@ int fwi_lbfgs_direction(void *ctx, int m, double *stats)
 {
     return ctx ? as_ctx(ctx)->lbfgs_direction(m, stats) : FWI_ERR_ARG;
 }
+int fwi_set_lbfgs_guard(void *ctx, int on)
+{
+    if (!ctx) return FWI_ERR_ARG;
+    as_ctx(ctx)->set_lbfgs_guard(on);
+    return FWI_OK;
+}
+
 int fwi_get_config(void *ctx, fwi_config *out)
 {
     if (!ctx || !out) return FWI_ERR_ARG;

@@ -56,7 +56,8 @@ class Config(C.Structure):
 class InvertOpts(C.Structure):
     _fields_ = [("iterations", C.c_int), ("lbfgs_m", C.c_int), ("first_alpha", C.c_float * 3),
                 ("alpha0", C.c_float), ("max_halvings", C.c_int), ("reset_alpha", C.c_int),
-                ("flag_min", C.c_int), ("flag_max", C.c_int), ("armijo_c1", C.c_double)]
+                ("flag_min", C.c_int), ("flag_max", C.c_int), ("armijo_c1", C.c_double),
+                ("curvature_guard", C.c_int)]
 
 
 class PhaseChoice(C.Structure):
@@ -136,6 +137,7 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_invert_bands", [_p, shotp, _i, _p, _f, _f, _i, _i, BandObsFn, _p, C.POINTER(InvertOpts), _i,
                                      _p, _p])
         _sig(L, "fwi_direction_slope", [_p, _p])
+        _sig(L, "fwi_set_lbfgs_guard", [_p, _i])
         _sig(L, "fwi_load_model_files", [_p, C.c_char_p, C.c_char_p, C.c_char_p])
         _sig(L, "fwi_save_model_files", [_p, C.c_char_p, C.c_char_p, C.c_char_p])
         _sig(L, "fwi_set_frequency", [_p, _f, _i])
@@ -336,6 +338,10 @@ class Context:
                                       int(nt), fn, None, C.byref(o), 1 if restart_model else 0,
                                       hist.ctypes.data, done.ctypes.data), "fwi_invert_bands")
         return [hist[b * o.iterations: b * o.iterations + done[b]] for b in range(nbands)]
+
+    def set_lbfgs_guard(self, on=True):
+        """Skip history pairs without positive curvature in later L-BFGS directions."""
+        _check(lib().fwi_set_lbfgs_guard(self._h, 1 if on else 0), "fwi_set_lbfgs_guard")
 
     def direction_slope(self):
         out = np.zeros(3, np.float64)

@@ -154,6 +154,14 @@ int fwi_first_step(void *ctx, float a_hor, float a_po, float a_nmo);
  * of the newest pair. */
 int fwi_lbfgs_direction(void *ctx, int m, double *stats);
 
+/* Curvature safeguard of the two-loop recursion (no counterpart in the reference, whose
+ * two-loop uses every pair: src/main.c:574-681).  With on != 0, later directions skip, per
+ * parameter, every history pair whose y.s <= 0 (the gradient did not grow along the step, so
+ * the pair carries no positive curvature and 1/(y.s) would turn the direction uphill), and
+ * scale the initial matrix by the newest pair with y.s > 0, or by |s| / |y| of the newest pair
+ * when there is none.  0 (the default) reproduces the reference. */
+int fwi_set_lbfgs_guard(void *ctx, int on);
+
 /* Trial model m = m_back - alpha r below the layer, optional clamps, v_hor >= v_nmo
  * (src/parallelcalls.cu:343-404). */
 int fwi_lbfgs_update(void *ctx, float alpha_v, float alpha_d, float alpha_e, int flag_min,
@@ -184,6 +192,8 @@ typedef struct {
     int flag_min, flag_max; /* clamps of update_LBFGS (src/parallelcalls.cu:343-404) */
     double armijo_c1;     /* 0: the reference's acceptance (trial misfit below the iteration's);
                              > 0: also J_trial <= J - c1 alpha sum(fwi_direction_slope), FP64 */
+    int curvature_guard;  /* fwi_set_lbfgs_guard for the band's directions (0: the reference's
+                             two-loop, every pair) */
 } fwi_invert_opts;
 
 void fwi_invert_defaults(fwi_invert_opts *opts);

@@ -38,8 +38,10 @@ def compat_gradient_shot(L, nx, nz, nt, cpml, dh, dt, ax, bx, az, bz, vh, vp, vn
     rt, s1 = _blocking_stream()
     _, s2 = _blocking_stream()
     n = nx * nz
-    dh2 = np.float32(dh * dh)
-    C_ = float(np.float32(np.float32(dt * dt) / dh2))
+    # C = (dt * dt) / dh2 in FP32 operations, as src/main.c:55 forms it from float dt and dh
+    f32 = np.float32
+    dh2 = f32(f32(dh) * f32(dh))
+    C_ = float(f32(f32(dt) * f32(dt)) / dh2)
     a_x, b_x, a_z, b_z = (dev(a) for a in (ax, bx, az, bz))
     v_hor, v_po, v_nmo = dev(vh), dev(vp), dev(vn)
     src = dev(source)

@@ -197,6 +197,12 @@ int fwi_lbfgs_direction(void *ctx, int m, double *stats)
     return FWI_OK;
 }
 
+int fwi_set_lbfgs_guard(void *ctx, int on)
+{
+    (void)ctx; (void)on;  /* the stand-in's direction is a scaled gradient: no pairs to guard */
+    return FWI_OK;
+}
+
 int fwi_direction_slope(void *ctx, double *out3)
 {
     mock_ctx *c = (mock_ctx *)ctx;

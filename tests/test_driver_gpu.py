@@ -162,3 +162,35 @@ def test_model_files_round_trip(tmp_path):
         assert np.array_equal(np.fromfile(p, np.float32).reshape(NZ, NX), a)
     with pytest.raises(fwi_gb300.FwiError):
         ctx.load_model_files(paths[0], paths[1], str(tmp_path / "missing.bin"))
+
+
+def test_curvature_guard_keeps_the_direction_downhill():
+    """A history pair with y.s < 0 for one parameter: the reference's two-loop
+    (no guard) scales that parameter's direction by a negative gamma, uphill;
+    fwi_set_lbfgs_guard skips the pair, and every parameter's direction is a
+    descent direction (g . r > 0 on the rows the update changes)."""
+    rng = np.random.default_rng(3)
+    m0 = [G["vh_i"], G["vp_i"], G["vn_i"]]
+    g0 = [rng.standard_normal((NZ, NX)).astype(np.float32) for _ in range(3)]
+    stats = {}
+    for guard in (False, True):
+        ctx, _, _ = make_ctx()
+        ctx.set_model(*m0)
+        ctx.set_gradient(*g0)
+        ctx.first_step(3e5, 2e5, 2.5e5)
+        m1 = ctx.get_model()
+        s = [a.astype(np.float64) - b for a, b in zip(m1, m0)]
+        # v_hor: the gradient falls along the step (y.s < 0); v_po, v_nmo: it grows (y.s > 0)
+        k = [-1e-6, 1e-6, 1e-6]
+        g1 = [(g + kk * sv).astype(np.float32) for g, kk, sv in zip(g0, k, s)]
+        ctx.set_gradient(*g1)
+        ctx.set_lbfgs_guard(guard)
+        st = ctx.lbfgs_direction(5)
+        slope = ctx.direction_slope()
+        stats[guard] = (st, slope)
+    (st0, sl0), (st1, sl1) = stats[False], stats[True]
+    assert st0[6] < 0 < st0[7] and st0[8] > 0      # y.s of the newest pair, v_hor negative
+    assert st0[0] < 0                               # unguarded gamma for v_hor: negative
+    assert sl0[0] < 0                               # ... so its direction points uphill
+    assert np.all(st1[0:3] > 0) and np.all(np.asarray(sl1) > 0)
+    np.testing.assert_allclose(st1[1:3], st0[1:3], rtol=1e-12)  # the other parameters unchanged
