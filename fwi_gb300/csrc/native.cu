@@ -674,6 +674,10 @@ template <typename T> struct Ctx : CtxBase {
                               (const void *)b.mn, (const void *)b.cpa, (const void *)b.cpb, (const void *)b.wavelet,
                               (const void *)b.status, b.tma})
             key_add(k, p);
+        for (int l = 0; l < 4; l++) {
+            key_add(k, (const void *)b.tiles[l]);
+            key_add(k, (long)b.ntiles[l]);
+        }
         for (const T *p : b.lvl) key_add(k, (const void *)p);
         for (const T *p : b.cp) key_add(k, (const void *)p);
         for (const T *p : b.g) key_add(k, (const void *)p);
@@ -768,6 +772,7 @@ template <typename T> struct Ctx : CtxBase {
         if (st) cudaStreamSynchronize(st);
         drop_sections();
         for (void *p : allocs) cudaFree(p);
+        for (const TileListEntry &e : tile_lists) cudaFree(e.dev);
         if (ss.side) cudaStreamSynchronize(ss.side);
         if (rst) cudaStreamSynchronize(rst);
         for (auto &e : ev)
@@ -1063,7 +1068,49 @@ template <typename T> struct Ctx : CtxBase {
             b.inline_strip = tg.inline_strip && c.inline_strip;
             if (const char *e = getenv("FWI_INLINE_STRIP"))  // 0: the strip pass path (tests)
                 if (atoi(e) == 0) b.inline_strip = 0;
+            // one block per tile of each pass's role (the exact adjoint's layers reach 4 points further)
+            const int aw_adj = cfg.mode == FWI_MODE_EXACT ? cfg.cpml + fwi::kRad : cfg.cpml;
+            const int role_aw[4][2] = {{1, cfg.cpml}, {2, cfg.cpml}, {1, aw_adj}, {2, aw_adj}};
+            for (int l = 0; l < 4; l++)
+                b.tiles[l] = tile_list(nxm, b.xbase, b.zbase, role_aw[l][1], role_aw[l][0], b.ntiles[l]);
         }
+    }
+
+    // Device copies of the compact tile lists (Batch::tiles), one per window width, grid
+    // origin, layer width and role, made on first use and kept for the context's life (a
+    // captured graph reads them).  Null (full grid) if the list cannot be made.
+    struct TileListEntry {
+        int nxm, xbase, zbase, aw, role, n;
+        int *dev;
+    };
+    mutable std::vector<TileListEntry> tile_lists;
+    const int *tile_list(int nxm, int xbase, int zbase, int aw, int role, int &n) const
+    {
+        for (const TileListEntry &e : tile_lists)
+            if (e.nxm == nxm && e.xbase == xbase && e.zbase == zbase && e.aw == aw && e.role == role) {
+                n = e.n;
+                return e.dev;
+            }
+        std::vector<int> t;
+        for (int tz = 0; zbase + tz * fwi::kTileEdge < nz; tz++)
+            for (int tx = 0; xbase + tx * fwi::kTileEdge < nxm; tx++)
+                if (fwi::tile_role(xbase + tx * fwi::kTileEdge, zbase + tz * fwi::kTileEdge, nxm, nz, aw) == role)
+                    t.push_back(tx | (tz << 16));
+        n = (int)t.size();
+        int *d = nullptr;
+        if (t.empty() || cudaMalloc(&d, t.size() * sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+            return nullptr;
+        }
+        if (cudaMemcpy(d, t.data(), t.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(d);
+            n = 0;
+            return nullptr;
+        }
+        tile_lists.push_back({nxm, xbase, zbase, aw, role, n, d});
+        return d;
     }
 
     // CPML table by distance (src/main.c:48-51: L = CPML dh, d0 = -3 ln R / (2 L), in T)
@@ -1208,6 +1255,10 @@ template <typename T> struct Ctx : CtxBase {
         b.inline_strip = 0;
         b.mixed = 0;
         b.tma = use_tma ? (const void *)&maps : nullptr;
+        for (int l = 0; l < 4; l++) {
+            b.tiles[l] = nullptr;
+            b.ntiles[l] = 0;
+        }
         return b;
     }
 

@@ -48,7 +48,16 @@ template <typename T> struct Batch {
                             // MIXED kernels); the layer passes then take one shot per block
     int inline_strip;       // FP32: the layer tiles advance the CPML memory variables
     const void *tma;        // host copy of the batch's TMA tensor maps (FP32 path), or null
+    // Compact tile lists of the FP32 tile passes when every shot has one window: for each
+    // pass (TileList), the tiles of its role, packed tx | tz << 16 on the grid from (xbase,
+    // zbase); one block per listed tile and shot group.  Null: the full tile grid, whose
+    // blocks on tiles of another role return at once (groups of several windows).
+    const int *tiles[4];
+    int ntiles[4];
 };
+
+// The tile lists of Batch::tiles.
+enum TileList { kTilesFwdInterior = 0, kTilesFwdLayer = 1, kTilesAdjInterior = 2, kTilesAdjLayer = 3 };
 
 // Shots of a batch run end-aligned on one global clock of `ntb` steps (the
 // batch's longest shot): shot s does its local step it = g - (ntb - nt_s),

@@ -27,6 +27,13 @@ inline dim3 tma_grid(const Batch<float> &b, int nx_max, int sg)
     return dim3((nx_max - b.xbase + TT - 1) / TT, (b.nz - b.zbase + TT - 1) / TT, (b.B + sg - 1) / sg);
 }
 
+// Blocks of one tile pass: one per tile of its compact list and shot group, or the full grid.
+inline dim3 pass_grid(const Batch<float> &b, int nx_max, int sg, int list)
+{
+    if (b.tiles[list]) return dim3(b.ntiles[list], 1, (b.B + sg - 1) / sg);
+    return tma_grid(b, nx_max, sg);
+}
+
 template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
 {
     const size_t sm = fwd_tma_smem();
@@ -34,14 +41,15 @@ template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, in
     if (b.mixed)
         k_fwd_tma<ST, true><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, g, ntb, cur, slot, b.sg);
     else
-        k_fwd_tma<ST, false><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, g, ntb, cur, slot, b.sg);
+        k_fwd_tma<ST, false><<<pass_grid(b, nx_max, b.sg, kTilesFwdInterior), kTmaThreads, sm, st>>>(b, m, g, ntb,
+                                                                                                   cur, slot, b.sg);
 }
 
 template <int ST, bool EXACT, bool INLINE>
 void fwd_layer(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
 {
     const size_t sm = fwd_layer_smem();
-    k_fwd_layer<ST, EXACT, INLINE><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
+    k_fwd_layer<ST, EXACT, INLINE><<<pass_grid(b, nx_max, b.sg_layer, kTilesFwdLayer), kTmaThreads, sm, st>>>(
         b, *static_cast<const TmaMaps *>(b.tma), g, ntb, cur, slot, b.sg_layer);
 }
 
@@ -54,15 +62,15 @@ void adj_interior(const Batch<float> &b, int nx_max, int j, int ntb, int cur, in
         k_adj_tma<ST, EXACT, true><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, j, ntb, cur, zsel, base,
                                                                                        b.sg);
     else
-        k_adj_tma<ST, EXACT, false><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, j, ntb, cur, zsel, base,
-                                                                                        b.sg);
+        k_adj_tma<ST, EXACT, false><<<pass_grid(b, nx_max, b.sg, kTilesAdjInterior), kTmaThreads, sm, st>>>(
+            b, m, j, ntb, cur, zsel, base, b.sg);
 }
 
 template <int ST, bool EXACT, bool INLINE>
 void adj_layer(const Batch<float> &b, int nx_max, int j, int ntb, int cur, int zsel, int base, cudaStream_t st)
 {
     const size_t sm = adj_layer_smem();
-    k_adj_layer<ST, EXACT, INLINE><<<tma_grid(b, nx_max, b.sg_layer), kTmaThreads, sm, st>>>(
+    k_adj_layer<ST, EXACT, INLINE><<<pass_grid(b, nx_max, b.sg_layer, kTilesAdjLayer), kTmaThreads, sm, st>>>(
         b, *static_cast<const TmaMaps *>(b.tma), j, ntb, cur, zsel, base, b.sg_layer);
 }
 

@@ -86,7 +86,8 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
     __shared__ int act[kMaxGroup];
     __shared__ FwdShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
+    int x0, z0;
+    tile_origin(b, kTilesFwdLayer, x0, z0);
     const DevShot gsh = b.shots[blockIdx.z * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
     if (tile_role(x0, z0, nx, nz, cpml) != 2) return;
@@ -114,7 +115,7 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
         q.sc = 1.f;
         if (img_slot >= 0 && Cd::scaled) {
             q.sc = image_scale(b.amax[(long)s * (b.nt_max + 1) + g], (float)b.inv_dh2);
-            if (blockIdx.x == 0 && blockIdx.y == 0) b.scale[(long)s * b.nt_max + g] = q.sc;  // tile (0, 0)
+            if (x0 == b.xbase && z0 == b.zbase) b.scale[(long)s * b.nt_max + g] = q.sc;  // tile (0, 0)
         }
         ps[tid] = q;
     }
@@ -347,7 +348,8 @@ k_adj_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb
     __shared__ int act[kMaxGroup];
     __shared__ AdjShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
+    int x0, z0;
+    tile_origin(b, kTilesAdjLayer, x0, z0);
     const int grp = blockIdx.z;
     const DevShot gsh = b.shots[grp * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;

@@ -151,6 +151,21 @@ __device__ __forceinline__ float d2_col(const float4 *v, int q)
            C::d2_4 * ((comp(v[8], q) - o) + (comp(v[0], q) - o));
 }
 
+// Origin of this block's tile: the list entry blockIdx.x of Batch::tiles[list], or grid
+// position (blockIdx.x, blockIdx.y) without a list.
+__device__ __forceinline__ void tile_origin(const Batch<float> &b, int list, int &x0, int &z0)
+{
+    const int *t = b.tiles[list];
+    if (t) {
+        const int v = t[blockIdx.x];
+        x0 = b.xbase + (v & 0xffff) * TT;
+        z0 = b.zbase + (v >> 16) * TT;
+    } else {
+        x0 = b.xbase + blockIdx.x * TT;
+        z0 = b.zbase + blockIdx.y * TT;
+    }
+}
+
 // Max over the warp, one atomic per warp (values are >= 0).
 __device__ __forceinline__ void warp_max_to(float v, float *dst)
 {
@@ -219,7 +234,8 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     __shared__ int act[kMaxGroup];
     __shared__ FwdShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
+    int x0, z0;
+    tile_origin(b, kTilesFwdInterior, x0, z0);
     const DevShot gsh = b.shots[blockIdx.z * sg];  // unless MIXED, every shot of the group has this window
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
     if (!MIXED && tile_role(x0, z0, nx, nz, cpml) != 1) return;
@@ -242,7 +258,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
         q.sc = 1.f;
         if (img_slot >= 0 && Cd::scaled) {
             q.sc = image_scale(b.amax[(long)s * (b.nt_max + 1) + g], (float)b.inv_dh2);
-            if (blockIdx.x == 0 && blockIdx.y == 0) b.scale[(long)s * b.nt_max + g] = q.sc;  // a layer tile
+            if (x0 == b.xbase && z0 == b.zbase) b.scale[(long)s * b.nt_max + g] = q.sc;  // never: a layer tile
         }
         ps[tid] = q;
     }
@@ -422,7 +438,8 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     __shared__ int act[kMaxGroup];
     __shared__ AdjShot ps[kMaxGroup];
     const int tid = threadIdx.x;
-    const int x0 = b.xbase + blockIdx.x * TT, z0 = b.zbase + blockIdx.y * TT;
+    int x0, z0;
+    tile_origin(b, kTilesAdjInterior, x0, z0);
     const int grp = blockIdx.z;
     const DevShot gsh = b.shots[grp * sg];
     const int nx = gsh.nx, nz = b.nz, pitch = b.pitch, cpml = b.cpml;
