@@ -69,7 +69,9 @@ struct HostTmaMaps {
     CUtensorMap fz[2];
     CUtensorMap mx[8];
     CUtensorMap mz[8];
+    CUtensorMap inc[2];
 };
+static_assert(sizeof(HostTmaMaps) == 26 * sizeof(CUtensorMap), "HostTmaMaps mirrors TmaMaps");
 
 }  // namespace fwi
 
@@ -932,6 +934,10 @@ template <typename T> struct Ctx : CtxBase {
             int rc = make_tensor_map_3d(&m.px[k], lv[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 40, 32, 1);
             if (rc) return rc;
             rc = make_tensor_map_3d(&m.fz[k], lv[2 + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 32, 40, 1);
+            if (rc) return rc;
+        }
+        for (int k = 0; k < 2; k++) {  // P, F increments without a halo (forward interior tiles)
+            int rc = make_tensor_map_3d(&m.inc[k], lv[4 + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pitch, nz, B, 32, 32, 1);
             if (rc) return rc;
         }
         for (int k = 0; k < 8; k++) {  // CPML memory variables, both halo shapes (layer tiles)

@@ -14,6 +14,9 @@
 
 namespace fwi {
 
+// native.cu fills a host copy of TmaMaps with the same members in the same order
+static_assert(sizeof(TmaMaps) == 26 * sizeof(CUtensorMap), "TmaMaps layout");
+
 namespace {
 
 template <typename K> cudaError_t allow_smem(K kernel, size_t bytes)
@@ -36,7 +39,7 @@ inline dim3 pass_grid(const Batch<float> &b, int nx_max, int sg, int list)
 
 template <int ST> void fwd_interior(const Batch<float> &b, int nx_max, int g, int ntb, int cur, int slot, cudaStream_t st)
 {
-    const size_t sm = fwd_tma_smem();
+    const size_t sm = fwd_tma_smem(b.sg);
     const TmaMaps &m = *static_cast<const TmaMaps *>(b.tma);
     if (b.mixed)
         k_fwd_tma<ST, true><<<tma_grid(b, nx_max, b.sg), kTmaThreads, sm, st>>>(b, m, g, ntb, cur, slot, b.sg);
@@ -150,8 +153,8 @@ template <int ST> cudaError_t allow_all()
 {
     cudaError_t e = cudaSuccess;
     auto keep = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
-    keep(allow_smem(k_fwd_tma<ST, false>, fwd_tma_smem()));
-    keep(allow_smem(k_fwd_tma<ST, true>, fwd_tma_smem()));
+    keep(allow_smem(k_fwd_tma<ST, false>, fwd_tma_smem(kMaxGroup)));
+    keep(allow_smem(k_fwd_tma<ST, true>, fwd_tma_smem(kMaxGroup)));
     keep(allow_smem(k_fwd_layer<ST, true, true>, fwd_layer_smem()));
     keep(allow_smem(k_fwd_layer<ST, true, false>, fwd_layer_smem()));
     keep(allow_smem(k_fwd_layer<ST, false, true>, fwd_layer_smem()));

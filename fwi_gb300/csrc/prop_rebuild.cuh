@@ -169,6 +169,6 @@ k_rebuild_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int n
     }
 }
 
-inline size_t rebuild_tma_smem() { return fwd_tma_smem(); }
+inline size_t rebuild_tma_smem() { return 128 + kStages * sizeof(FwdStage); }
 
 }  // namespace fwi

@@ -34,6 +34,7 @@ struct TmaMaps {
     CUtensorMap fz[2];   // F level 0/1: 32 x 40 boxes (z-halo)
     CUtensorMap mx[8];   // CPML memory variables cp[k]: 40 x 32 boxes (x-halo)
     CUtensorMap mz[8];   // the same, 32 x 40 boxes (z-halo)
+    CUtensorMap inc[2];  // P and F increments (levels 4, 5): 32 x 32 boxes, no halo
 };
 
 // Only the fields read with a halo are staged; the increments and images,
@@ -43,6 +44,16 @@ struct TmaMaps {
 struct FwdStage {
     float P[TT][TH];
     float F[TH][TT];
+};
+
+// The forward interior tiles also stage the tile's P and F increments (the
+// thread's own points, no halo), so that every state read of a shot is an
+// asynchronous copy issued kStages shots ahead.
+struct FwdIncStage {
+    float P[TT][TH];
+    float F[TH][TT];
+    float VP[TT][TT];
+    float VF[TT][TT];
 };
 
 struct AdjStage {
@@ -228,11 +239,14 @@ __global__ void __launch_bounds__(kTmaThreads, 4)
 k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, int cur, int img_slot, int sg)
 {
     using Cd = Codec<float, ST>;
+    // dynamic shared memory: the stages, then the group's per-shot scalars and active shots (sized
+    // by the group, so that a small group leaves room for a fourth block on the SM)
     extern __shared__ __align__(128) unsigned char dsm_raw[];
-    FwdStage *stage = reinterpret_cast<FwdStage *>(aligned_dsm(dsm_raw));
+    unsigned char *dsm = aligned_dsm(dsm_raw);
+    FwdIncStage *stage = reinterpret_cast<FwdIncStage *>(dsm);
+    FwdShot *ps = reinterpret_cast<FwdShot *>(dsm + kStages * sizeof(FwdIncStage));
+    int *act = reinterpret_cast<int *>(ps + sg);
     __shared__ __align__(8) uint64_t bar[kStages];
-    __shared__ int act[kMaxGroup];
-    __shared__ FwdShot ps[kMaxGroup];
     const int tid = threadIdx.x;
     int x0, z0;
     tile_origin(b, kTilesFwdInterior, x0, z0);
@@ -265,11 +279,13 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     __syncthreads();
     auto issue = [&](int a) {
         const int s = act[a];
-        FwdStage &S = stage[a % kStages];
+        FwdIncStage &S = stage[a % kStages];
         uint64_t *br = &bar[a % kStages];
-        mbar_expect_tx(br, (unsigned)sizeof(FwdStage));
+        mbar_expect_tx(br, (unsigned)sizeof(FwdIncStage));
         tma_load_3d(S.P, &maps.px[cur], br, x0 - kRad, z0, s);
         tma_load_3d(S.F, &maps.fz[cur], br, x0, z0 - kRad, s);
+        tma_load_3d(S.VP, &maps.inc[0], br, x0, z0, s);
+        tma_load_3d(S.VF, &maps.inc[1], br, x0, z0, s);
     };
     if (tid == 0)
         for (int k = 0; k < min(kStages, na); k++) issue(k);
@@ -295,24 +311,20 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     for (int a = 0; a < na; a++) {
         const FwdShot &sh = ps[a];
         const long so = sh.so;
-        float4 vP = make_float4(0.f, 0.f, 0.f, 0.f), vF = vP;
-        if (any) {  // own points only: issued before the wait, in flight during it
-            vP = ld4(Pv0 + so + ipt);
-            vF = ld4(Fv0 + so + ipt);
-            if (MIXED) {  // this shot's model columns
-                const long mi = (long)iz * b.mpitch + sh.wx0 + ix0;
+        if (MIXED && any) {  // this shot's model columns: issued before the wait, in flight during it
+            const long mi = (long)iz * b.mpitch + sh.wx0 + ix0;
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    mh[q] = m[q] ? b.mh[mi + q] : 0.f;
-                    mp[q] = m[q] ? b.mp[mi + q] : 0.f;
-                    mn[q] = m[q] ? b.mn[mi + q] : 0.f;
-                }
+            for (int q = 0; q < 4; q++) {
+                mh[q] = m[q] ? b.mh[mi + q] : 0.f;
+                mp[q] = m[q] ? b.mp[mi + q] : 0.f;
+                mn[q] = m[q] ? b.mn[mi + q] : 0.f;
             }
         }
         const bool ok = mbar_wait(&bar[a % kStages], (a / kStages) & 1);
-        const FwdStage &S = stage[a % kStages];
+        const FwdIncStage &S = stage[a % kStages];
         float lmax = 0.f;
         if (any && ok) {
+            const float4 vP = ld4(&S.VP[r][c4]), vF = ld4(&S.VF[r][c4]);
             float pv[12];
             {
                 const float *row = &S.P[r][c4];
@@ -663,7 +675,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     }
 }
 
-inline size_t fwd_tma_smem() { return 128 + kStages * sizeof(FwdStage); }
+inline size_t fwd_tma_smem(int sg) { return 128 + kStages * sizeof(FwdIncStage) + sg * (sizeof(FwdShot) + sizeof(int)); }
 inline size_t adj_tma_smem()
 {
     return 128 + kAdjStages * sizeof(AdjStage) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
