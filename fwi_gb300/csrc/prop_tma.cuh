@@ -61,8 +61,16 @@ struct AdjStage {
     float F[TH][TH];
 };
 
+// The adjoint interior tiles also stage the tile's lambda increments (own points, no halo).
+struct AdjIncStage {
+    float P[TH][TH];
+    float F[TH][TH];
+    float WP[TT][TT];
+    float WF[TT][TT];
+};
+
 constexpr int kStages = 3;     // TMA pipeline depth over a group's shots (forward interior tiles)
-constexpr int kAdjStages = 2;  // adjoint interior tiles: 2 stages keep 4 blocks on an SM
+constexpr int kAdjStages = 2;  // adjoint interior tiles: 2 stages keep 3 blocks on an SM
 
 __device__ __forceinline__ unsigned char *aligned_dsm(unsigned char *p)
 {
@@ -431,12 +439,12 @@ struct AdjShot {
 // staged per shot, at the shot's own columns, and each shot's imaging goes
 // to its own gradient slot (shot s: slot s) instead of a sum per group.
 template <int ST, bool EXACT, bool MIXED>
-__global__ void __launch_bounds__(kTmaThreads, 4)
+__global__ void __launch_bounds__(kTmaThreads, 3)
 k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, int cur, int zsel, int img_base,
           int sg)
 {
     using Cd = Codec<float, ST>;
-    using Stage = AdjStage;
+    using Stage = AdjIncStage;
     using SI = typename Cd::S;
     extern __shared__ __align__(128) unsigned char dsm_raw[];
     unsigned char *dsm = aligned_dsm(dsm_raw);
@@ -486,6 +494,8 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
         mbar_expect_tx(br, (unsigned)sizeof(Stage));
         tma_load_3d(S.P, &maps.lvl[cur], br, x0 - kRad, z0 - kRad, s);
         tma_load_3d(S.F, &maps.lvl[2 + cur], br, x0 - kRad, z0 - kRad, s);
+        tma_load_3d(S.WP, &maps.inc[0], br, x0, z0, s);
+        tma_load_3d(S.WF, &maps.inc[1], br, x0, z0, s);
     };
     if (tid == 0)
         for (int k = 0; k < min(kAdjStages, na); k++) issue(k);
@@ -527,13 +537,10 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
     float *const lPw0 = b.lvl[4], *const lFw0 = b.lvl[5];
     float ah[4] = {0.f, 0.f, 0.f, 0.f}, ap[4] = {0.f, 0.f, 0.f, 0.f}, an[4] = {0.f, 0.f, 0.f, 0.f};
     for (int a = 0; a < na; a++) {
-        // own points' increments and images: issued before the wait, in flight during it
-        float4 wP = make_float4(0.f, 0.f, 0.f, 0.f), wF = wP;
+        // own points' images: issued before the wait, in flight during it (the increments come
+        // with the stage)
         SI iG[4], iH[4];
         if (any) {
-            const long so = ps[a].so;
-            wP = ld4(lPw0 + so + ipt);
-            wF = ld4(lFw0 + so + ipt);
             if (ps[a].img >= 0) {
                 const SI *img = (const SI *)b.store + ps[a].img;
                 Vec4Store<SI>::get(img + ipt, iG);
@@ -581,7 +588,8 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
                 e[q][0] = d2_row(uv, q) * b.inv_dh2;
                 e[q][1] = d2_col(vz, q) * b.inv_dh2;
             }
-            const bool rec_row = iz == sh.rz;
+                const bool rec_row = iz == sh.rz;
+            const float4 wP = ld4(&S.WP[r][c4]), wF = ld4(&S.WF[r][c4]);
             float nwP[4], nwF[4], nP[4], nF[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -678,7 +686,7 @@ k_adj_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int j, int ntb, 
 inline size_t fwd_tma_smem(int sg) { return 128 + kStages * sizeof(FwdIncStage) + sg * (sizeof(FwdShot) + sizeof(int)); }
 inline size_t adj_tma_smem()
 {
-    return 128 + kAdjStages * sizeof(AdjStage) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
+    return 128 + kAdjStages * sizeof(AdjIncStage) + sizeof(float) * (2 * TT * TH + TH * TT + TT * TH + TH * TT);
 }
 
 }  // namespace fwi
