@@ -1383,19 +1383,29 @@ template <typename T> struct Ctx : CtxBase {
                 }
                 return k;
             };
+            // checkpoint storage: the last two segments' images fit the two-segment image buffer, so
+            // the forward writes them there itself; the adjoint starts on them at once and only the
+            // segments before them are recomputed from their checkpoints
+            const int last_seg = ckpt ? (ntb - 1) / ck_every : 0;
+            const int first_direct = ckpt ? std::max(0, last_seg - 1) : 0;
+            auto fwd_img_slot = [&](int g) {
+                if (!want_grad || bnd) return -1;
+                if (!ckpt) return g;
+                const int seg = g / ck_every;
+                return seg >= first_direct ? g - seg * ck_every + (seg & 1) * ck_every : -1;
+            };
             NvtxRange fwd_range("fwi forward steps");
             rc = run_section(section_key(0), 0, nsamp, spts[0], [&]() -> int {
                 int cur = 0;
                 for (int g = 0; g < ntb; g++) {
-                    if (ckpt && g % ck_every == 0) {
+                    if (ckpt && g % ck_every == 0 && g / ck_every < first_direct) {
                         int rc2 = save_checkpoint(g / ck_every, nb, cur);
                         if (rc2) return rc2;
                     }
                     fwi::StepStreams sst = ss;
                     sample(0, g, sst);
                     if (bnd) fwi::launch_save_ring<T>(bf, nxm, g, ntb, cur, ring, ring_len, st);
-                    fwi::launch_forward_step<T>(bf, nxm, g, ntb, cur, (want_grad && !ckpt && !bnd) ? g : -1, exact,
-                                                sst);
+                    fwi::launch_forward_step<T>(bf, nxm, g, ntb, cur, fwd_img_slot(g), exact, sst);
                     cur ^= 1;
                 }
                 TRY_LAUNCH();
@@ -1516,14 +1526,13 @@ template <typename T> struct Ctx : CtxBase {
                             launches += kps * (e - a);
                             return FWI_OK;
                         };
-                        const int last = (ntb - 1) / ck_every;
-                        int rc3 = recompute(last);
-                        if (rc3) return rc3;
+                        // segments first_direct .. last_seg were imaged by the forward itself
+                        int rc3 = FWI_OK;
                         int j = 0;
-                        for (int seg = last; seg >= 0; seg--) {
+                        for (int seg = last_seg; seg >= 0; seg--) {
                             const int a = seg * ck_every, h = seg & 1;
-                            if (seg > 0 && (rc3 = recompute(seg - 1))) return rc3;
-                            TRY(cudaStreamWaitEvent(st, ev_reb[h], 0));
+                            if (seg > 0 && seg - 1 < first_direct && (rc3 = recompute(seg - 1))) return rc3;
+                            if (seg < first_direct) TRY(cudaStreamWaitEvent(st, ev_reb[h], 0));
                             for (; j < ntb && ntb - 1 - lag - j >= a; j++) {
                                 fwi::StepStreams sst = ss;
                                 sample(1, j, sst);
