@@ -1714,17 +1714,29 @@ template <typename T> struct Ctx : CtxBase {
                 us = 1e3 * ms / K;
                 return FWI_OK;
             };
+            // a candidate's time: the median of three timed runs (single runs vary by a few
+            // per cent, about the differences between neighbouring choices)
+            auto timed = [&](const Choice &c, int ph, double &us) -> int {
+                double v[3];
+                for (double &x : v) {
+                    const int r = trial(c, ph, x);
+                    if (r) return r;
+                }
+                std::sort(v, v + 3);
+                us = v[1];
+                return FWI_OK;
+            };
             double t_best[2] = {0, 0}, t_dflt[2] = {0, 0}, t = 0;
             int trials = 0;
             for (int ph = 0; ph < 2; ph++) {
                 if ((rc = trial(dflt, ph, t))) return rc;  // warm-up
-                if ((rc = trial(dflt, ph, t_dflt[ph]))) return rc;
+                if ((rc = timed(dflt, ph, t_dflt[ph]))) return rc;
                 t_best[ph] = t_dflt[ph];
                 trials++;
                 Choice &bp = ph == 0 ? best.fwd : best.adj;
                 auto consider = [&](const Choice &c) -> int {
                     if (c == bp) return FWI_OK;
-                    const int r = trial(c, ph, t);
+                    const int r = timed(c, ph, t);
                     if (r) return r;
                     trials++;
                     if (t < 0.99 * t_best[ph]) {
@@ -1757,6 +1769,27 @@ template <typename T> struct Ctx : CtxBase {
                         c.inline_strip = !c.inline_strip;
                         if ((rc = consider(c))) return rc;
                     }
+                }
+                // the two group sizes interact (both passes share the SMs): every pair within two
+                // candidate steps of the best, which the one-at-a-time descent above can miss
+                if (uniform) {
+                    const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
+                    auto index_of = [&](int v) {
+                        for (int k = 0; k < ncand; k++)
+                            if (cand[k] == v) return k;
+                        return 0;
+                    };
+                    const Choice centre = bp;
+                    const int i0 = index_of(centre.sg), j0 = index_of(centre.sg_layer);
+                    for (int di = -2; di <= 2; di++)
+                        for (int dj = -2; dj <= 2; dj++) {
+                            const int i = i0 + di, jj = j0 + dj;
+                            if (i < 0 || jj < 0 || i >= ncand || jj >= ncand || cand[i] > nb || cand[jj] > nb) continue;
+                            Choice c = centre;
+                            c.sg = cand[i];
+                            c.sg_layer = cand[jj];
+                            if ((rc = consider(c))) return rc;
+                        }
                 }
             }
             record_choice(key, best);

@@ -260,8 +260,9 @@ long fwi_last_launches(void *ctx);
  * CPML memory variables themselves or after a strip pass; the forward and
  * the adjoint are chosen separately.  fwi_autotune times `steps` steps of
  * candidate choices of each phase for each batch the shots form (coordinate
- * descent from the built-in choice; a candidate must be 1 % faster to
- * replace it) and records the fastest per batch shape (shots in the batch,
+ * descent from the built-in choice, then every pair of group sizes near the
+ * best; each candidate timed three times, the median kept; a candidate must
+ * be 1 % faster to replace it) and records the fastest per batch shape (shots in the batch,
  * widest window, one window or several, mode, image type); later
  * fwi_gradient / fwi_misfit / fwi_forward calls on batches of that shape use
  * it.  Results stay within FP32 rounding of the built-in choice's; for a
