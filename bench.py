@@ -489,13 +489,42 @@ def reference_arm(args, rank, world, dist):
         vals.append(v)
     dt = time.perf_counter() - t0
     v = statistics.median(vals)
-    return {"metric": METRIC, "value": round(v, 6), "unit": "shots/s", "n_gpus": world, "steps": args.steps,
+    out = {"metric": METRIC, "value": round(v, 6), "unit": "shots/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "impl": "reference",
             "data": f"synthetic (seeded {args.workload} model)", "config": config_of(args, w),
             "cpu_baseline": {"value": round(v, 6), "unit": "shots/s", "cores": thr, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(v, 6), "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    ref_gpu = reference_gpu_kernels(w)
+    if ref_gpu:
+        out["reference_gpu_kernels"] = ref_gpu
+    return out
+
+
+def reference_gpu_kernels(w):
+    """The reference's own CUDA kernels (compiled unchanged for sm_103a into oracle/_ref where the
+    reference checkout was present at build time) on one GPU, one shot at a time as src/main.c runs
+    them (per-step snapshot through pinned host memory, host misfit sum): gradient shots/s of the
+    workload's first shot, for context beside the CPU figure.  None where they were not built."""
+    from oracle import pyoracle as po
+    if not po.ref_gpu_available():
+        return None
+    s = w.shots[0]
+    if s["nxw"]:
+        return None  # the reference has no shot windows
+    obs = np.zeros((s["nt"], w.nx), np.float32)  # the work does not depend on the data
+    try:
+        secs, _, _, _ = po.ref_gpu_shot(w.vel0, w.eps0, w.delta0, obs, w.nx, w.nz, s["nt"], w.cpml, w.dh, w.dt, w.f,
+                                        s["sx"] + 1, s["sz"] + 1, runs=3)
+    except Exception as e:  # noqa: BLE001 - reported, not fatal to the CPU arm
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    best = min(secs[1:])
+    return {"value": round(1.0 / best, 4), "unit": "shots/s", "seconds_per_shot": [round(x, 4) for x in secs],
+            "how": "src/parallelcalls.cu compiled for sm_103a with nvcc's defaults, one shot sequenced as "
+                   "src/main.c:318-495 (per-step snapshot via pinned host memory, residual summed on the host); "
+                   "best of the runs after the first; zero observed data (the work does not depend on it)",
+            "gpt_updates_per_s": round(2 * (w.nx - 8) * (w.nz - 8) * s["nt"] / best / 1e9, 3)}
 
 
 def main():

@@ -230,3 +230,30 @@ def lbfgs_direction(state, k, library=None):
           else lib().orc_lbfgs_direction_f32)
     fn(nx, nz, k, *[_ptr(state[n]) for n in names], _ptr(sig), _ptr(eps), _ptr(gam))
     return sig, eps, gam
+
+
+# ----------------------------------------------------------------- the reference's kernels on the GPU
+
+def ref_gpu_available() -> bool:
+    """The reference's kernels compiled for sm_103a and their shot driver exist (oracle/_ref)."""
+    return all(os.path.exists(os.path.join(HERE, "_ref", f)) for f in ("parallelcalls.cubin", "ref_gpu_shot"))
+
+
+def ref_gpu_shot(vel, eps, delta, obs, nx, nz, nt, cpml, dh, dt, f, sx, sz, runs=1):
+    """One shot of the reference's own CUDA kernels, sequenced as src/main.c:318-495
+    (oracle/ref_gpu/ref_gpu_shot.cpp): model (Vp, epsilon, delta) [nz][nx] and the
+    observed record [nt][nx] in, 1-based source (sx, sz).  Runs the shot `runs` times;
+    returns (seconds per run, misfit, (gcx, gcz, gdx), res)."""
+    import json
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        for name, a in (("vel", vel), ("eps", eps), ("delta", delta), ("obs", obs)):
+            np.ascontiguousarray(a, np.float32).tofile(os.path.join(d, f"{name}.f32"))
+        out = subprocess.run([os.path.join(HERE, "_ref", "ref_gpu_shot"), os.path.join(HERE, "_ref", "parallelcalls.cubin"),
+                              d, str(nx), str(nz), str(nt), str(cpml), repr(float(dh)), repr(float(dt)),
+                              repr(float(f)), str(sx), str(sz), str(runs)],
+                             capture_output=True, text=True, check=True).stdout
+        r = json.loads(out.strip().splitlines()[-1])
+        g = tuple(np.fromfile(os.path.join(d, f"{k}.f32"), np.float32).reshape(nz, nx) for k in ("gcx", "gcz", "gdx"))
+        res = np.fromfile(os.path.join(d, "res.f32"), np.float32).reshape(nt, nx)
+    return r["seconds_per_shot"], r["misfit"], g, res
