@@ -50,7 +50,8 @@ int fwi_invert(void *ctx, const fwi_shot *shots, int nshots, const void *obs, co
     fwi_invert_opts o;
     if (opts) o = *opts;
     else fwi_invert_defaults(&o);
-    if (!ctx || !shots || nshots <= 0 || !obs || o.iterations <= 0 || o.armijo_c1 < 0.0) return FWI_ERR_ARG;
+    /* obs == NULL: the records kept in the context (fwi_store_observed / fwi_model_observed) */
+    if (!ctx || !shots || nshots <= 0 || o.iterations <= 0 || o.armijo_c1 < 0.0) return FWI_ERR_ARG;
     float alpha = o.alpha0;
     int count = 0;
     int done = 0;
@@ -144,8 +145,9 @@ int fwi_invert_bands(void *ctx, const fwi_shot *shots, int nshots, const unsigne
         }
         rc = fwi_set_frequency(ctx, f, nt);
         if (rc != FWI_OK) break;
+        /* the band's records: the callback's, or (NULL) those it left in the context's store */
         const void *obs = NULL;
-        if (band_obs(user, b, f, &obs) != 0 || !obs) {
+        if (band_obs(user, b, f, &obs) != 0) {
             rc = FWI_ERR_ARG;
             break;
         }

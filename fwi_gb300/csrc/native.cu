@@ -211,6 +211,37 @@ __global__ void k_accumulate_gradient(T *gh, T *gp, T *gn, const T *sh_h, const 
     }
 }
 
+// ------------------------------------------------------------------ observed data kept on the device
+
+// Per-trace scale of a compact (FP16) record store: trace r of a shot is the column r of its
+// [nt][nrec] block.  scale = max |d| / 32768, so that every value maps below FP16's largest.
+template <typename T>
+__global__ void k_trace_scale(const T *d, long off, int nt, int nrec, float *scale)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    float m = 0.f;
+    for (int t = 0; t < nt; t++) m = fmaxf(m, fabsf((float)d[off + (long)t * nrec + r]));
+    scale[r] = m > 0.f ? m / 32768.f : 1.f;
+}
+
+template <typename T>
+__global__ void k_trace_encode(const T *d, long in_off, int nt, int nrec, const float *scale, __half *out,
+                               long out_off)
+{
+    const long n = (long)nt * nrec;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+        out[out_off + k] = __float2half_rn((float)d[in_off + k] / scale[k % nrec]);
+}
+
+template <typename T>
+__global__ void k_trace_decode(const __half *in, long off, int nt, int nrec, const float *scale, T *out, long out_off)
+{
+    const long n = (long)nt * nrec;
+    for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+        out[out_off + k] = (T)(__half2float(in[off + k]) * scale[k % nrec]);
+}
+
 // ------------------------------------------------------------------ L-BFGS on the device
 
 // Three-parameter dot products with a last-block-done FP64 reduction.
@@ -561,6 +592,9 @@ struct CtxBase {
     virtual int run(const fwi_shot *, int, const void *, const unsigned char *, void *, void *, void *,
                     double *, void *traces, bool grad) = 0;
     virtual int autotune(const fwi_shot *, int, int, fwi_tuning *) = 0;
+    virtual int store_observed(const fwi_shot *, int, const void *, int) = 0;
+    virtual int model_observed(const fwi_shot *, int, const void *, const void *, const void *, int) = 0;
+    virtual int free_observed() = 0;
     virtual int set_tuning(const fwi_shot *, int, const fwi_tuning *) = 0;
     virtual int check_bounded_wait(long polls) = 0;
     virtual int first_step(float, float, float) = 0;
@@ -768,6 +802,15 @@ template <typename T> struct Ctx : CtxBase {
     int lb_guard = 0;  // fwi_set_lbfgs_guard: skip pairs without positive curvature
     DotScratch ds{};
     T *vti_out[3] = {};
+    // observed data kept on the device (fwi_store_observed / fwi_model_observed): the records of
+    // the shots ostore_shots, laid out as fwi_gradient takes them, in FP32 (ostore) or FP16 with
+    // one scale per trace (ostore_h, ostore_scale; scale of trace r of shot k at moff[k] + r)
+    std::vector<fwi_shot> ostore_shots;
+    std::vector<long> ostore_off, ostore_moff;
+    T *ostore = nullptr;
+    __half *ostore_h = nullptr;
+    float *ostore_scale = nullptr;
+    T *ostore_tmp = nullptr, *model_keep[3] = {};
 
     ~Ctx() override
     {
@@ -775,6 +818,9 @@ template <typename T> struct Ctx : CtxBase {
         drop_sections();
         for (void *p : allocs) cudaFree(p);
         for (const TileListEntry &e : tile_lists) cudaFree(e.dev);
+        free_observed();
+        for (void *p : {(void *)ostore_tmp, (void *)model_keep[0], (void *)model_keep[1], (void *)model_keep[2]})
+            if (p) cudaFree(p);
         if (ss.side) cudaStreamSynchronize(ss.side);
         if (rst) cudaStreamSynchronize(rst);
         for (auto &e : ev)
@@ -1296,7 +1342,14 @@ template <typename T> struct Ctx : CtxBase {
     {
         if (!have_model || !have_wavelet) return FWI_ERR_STATE;
         if (!sh || n <= 0) return FWI_ERR_ARG;
-        if ((want_grad || misfit_out) && !obs_in) return FWI_ERR_ARG;
+        // without observed data from the caller: the records kept on the device, for the same shots
+        const bool from_store = (want_grad || misfit_out) && !obs_in;
+        if (from_store) {
+            if ((size_t)n != ostore_shots.size()) return FWI_ERR_ARG;
+            for (int k = 0; k < n; k++)
+                if (std::memcmp(&sh[k], &ostore_shots[k], sizeof(fwi_shot)) != 0) return FWI_ERR_ARG;
+        }
+        const bool have_obs = obs_in || from_store;
         std::vector<DevShot> all(n);
         std::vector<long> off(n + 1, 0), moff(n + 1, 0);
         for (int k = 0; k < n; k++) {
@@ -1333,6 +1386,17 @@ template <typename T> struct Ctx : CtxBase {
             TRY(cudaMemcpyAsync(mask_off, bmo.data(), nb * sizeof(long), cudaMemcpyHostToDevice, st));
             if (obs_in)
                 TRY(cudaMemcpyAsync(obs, (const T *)obs_in + off[b0], nrec_elems * sizeof(T), cudaMemcpyDefault, st));
+            else if (from_store && ostore)
+                TRY(cudaMemcpyAsync(obs, ostore + off[b0], nrec_elems * sizeof(T), cudaMemcpyDeviceToDevice, st));
+            else if (from_store)
+                for (int k = 0; k < nb; k++) {
+                    const int nr = all[b0 + k].rx1 - all[b0 + k].rx0;
+                    k_trace_decode<T><<<eg((long)all[b0 + k].nt * nr), 256, 0, st>>>(
+                        ostore_h, off[b0 + k], all[b0 + k].nt, nr, ostore_scale + moff[b0 + k], obs,
+                        off[b0 + k] - off[b0]);
+                    TRY_LAUNCH();
+                    launches++;
+                }
             if (mask_in)
                 TRY(cudaMemcpyAsync(mask, mask_in + moff[b0], moff[b0 + nb] - moff[b0], cudaMemcpyDefault, st));
             const size_t lb = (size_t)nb * slot * sizeof(T);
@@ -1424,7 +1488,7 @@ template <typename T> struct Ctx : CtxBase {
             });
             if (rc) return rc;
             TRY(cudaEventRecord(e1, st));
-            if (obs_in) {
+            if (have_obs) {
                 k_residual<T><<<dim3(red_blocks, nb), kRedThreads, 0, st>>>(rec, obs, mask_in ? mask : nullptr, shots,
                                                                           mask_off, partial);
                 k_misfit_finish<<<1, 256, 0, st>>>(partial, (long)nb * red_blocks, misfit);
@@ -1606,6 +1670,128 @@ template <typename T> struct Ctx : CtxBase {
         if (stat & fwi::kStatusSaturated) return FWI_ERR_NUMERIC;
         if (misfit_out && !std::isfinite(*misfit_out)) return FWI_ERR_NUMERIC;
         return FWI_OK;
+    }
+
+    // ---------------------------------------------------------------- observed data on the device
+
+    int free_observed() override
+    {
+        for (void *p : {(void *)ostore, (void *)ostore_h, (void *)ostore_scale})
+            if (p) cudaFree(p);
+        ostore = nullptr;
+        ostore_h = nullptr;
+        ostore_scale = nullptr;
+        ostore_shots.clear();
+        ostore_off.clear();
+        ostore_moff.clear();
+        return FWI_OK;
+    }
+
+    // Room for the records of these shots (offsets as fwi_gradient lays them out).
+    int observed_layout(const fwi_shot *sh, int n, int sprec)
+    {
+        if (!sh || n <= 0 || (sprec != FWI_SPREC_NATIVE && sprec != FWI_SPREC_FP16)) return FWI_ERR_ARG;
+        std::vector<long> off(n + 1, 0), moff(n + 1, 0);
+        for (int k = 0; k < n; k++) {
+            DevShot d;
+            int rc = check_shot(sh[k], d);
+            if (rc) return rc;
+            off[k + 1] = off[k] + (long)d.nt * (d.rx1 - d.rx0);
+            moff[k + 1] = moff[k] + (d.rx1 - d.rx0);
+        }
+        free_observed();
+        cudaError_t e = sprec == FWI_SPREC_NATIVE ? cudaMalloc(&ostore, off[n] * sizeof(T))
+                                                  : cudaMalloc(&ostore_h, off[n] * sizeof(__half));
+        if (e == cudaSuccess && sprec == FWI_SPREC_FP16) e = cudaMalloc(&ostore_scale, moff[n] * sizeof(float));
+        if (e != cudaSuccess) {
+            free_observed();
+            return fail(e);
+        }
+        ostore_shots.assign(sh, sh + n);
+        ostore_off = off;
+        ostore_moff = moff;
+        return FWI_OK;
+    }
+
+    // FP16 store: scales and codes of shots [k0, k0 + nk) from FP32 records at src (shot k at
+    // src_off + ostore_off[k] - ostore_off[k0]).
+    int encode_observed(const T *src, long src_base, int k0, int nk)
+    {
+        for (int k = k0; k < k0 + nk; k++) {
+            DevShot d;
+            check_shot(ostore_shots[k], d);
+            const int nr = d.rx1 - d.rx0;
+            const long so = src_base + ostore_off[k] - ostore_off[k0];
+            k_trace_scale<T><<<(nr + 127) / 128, 128, 0, st>>>(src, so, d.nt, nr, ostore_scale + ostore_moff[k]);
+            k_trace_encode<T><<<eg((long)d.nt * nr), 256, 0, st>>>(src, so, d.nt, nr, ostore_scale + ostore_moff[k],
+                                                                   ostore_h, ostore_off[k]);
+            TRY_LAUNCH();
+        }
+        return FWI_OK;
+    }
+
+    int store_observed(const fwi_shot *sh, int n, const void *obs_in, int sprec) override
+    {
+        if (!obs_in) return FWI_ERR_ARG;
+        int rc = observed_layout(sh, n, sprec);
+        if (rc) return rc;
+        const long total = ostore_off[n];
+        if (ostore) {
+            TRY(cudaMemcpyAsync(ostore, obs_in, total * sizeof(T), cudaMemcpyDefault, st));
+        } else {
+            // stage through a device copy when the records are in host memory
+            cudaPointerAttributes pa{};
+            const bool dev = cudaPointerGetAttributes(&pa, obs_in) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+            cudaGetLastError();
+            const T *src = (const T *)obs_in;
+            T *tmp = nullptr;
+            if (!dev) {
+                TRY(cudaMalloc(&tmp, total * sizeof(T)));
+                TRY(cudaMemcpyAsync(tmp, obs_in, total * sizeof(T), cudaMemcpyHostToDevice, st));
+                src = tmp;
+            }
+            rc = encode_observed(src, 0, 0, n);
+            TRY(cudaStreamSynchronize(st));
+            if (tmp) cudaFree(tmp);
+            if (rc) return rc;
+        }
+        TRY(cudaStreamSynchronize(st));
+        return FWI_OK;
+    }
+
+    // The records modelled on the device from the model (v_hor, v_po, v_nmo), straight into the
+    // store; the context's own model is kept.
+    int model_observed(const fwi_shot *sh, int n, const void *a, const void *b, const void *c, int sprec) override
+    {
+        if (!a || !b || !c) return FWI_ERR_ARG;
+        if (!have_wavelet) return FWI_ERR_STATE;
+        int rc = observed_layout(sh, n, sprec);
+        if (rc) return rc;
+        const bool had_model = have_model;
+        T *m3[3] = {vh, vp, vn};
+        for (int k = 0; k < 3; k++) {
+            if (!model_keep[k]) TRY(alloc(&model_keep[k], mslot));
+            TRY(cudaMemcpyAsync(model_keep[k], m3[k], mslot * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        }
+        if ((rc = set_model(a, b, c))) return rc;
+        if (ostore) {
+            rc = run(sh, n, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, ostore, false);
+        } else {
+            // FP16: model a batch at a time into FP32 scratch, then encode it
+            if (!ostore_tmp) TRY(alloc(&ostore_tmp, (size_t)B * nt_max * nrec_max));
+            for (int b0 = 0; b0 < n && rc == FWI_OK; b0 += B) {
+                const int nb = std::min(B, n - b0);
+                rc = run(sh + b0, nb, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, ostore_tmp, false);
+                if (rc == FWI_OK) rc = encode_observed(ostore_tmp, 0, b0, nb);
+            }
+        }
+        for (int k = 0; k < 3; k++)
+            TRY(cudaMemcpyAsync(m3[k], model_keep[k], mslot * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        have_model = had_model;
+        models_dirty = true;
+        TRY(cudaStreamSynchronize(st));
+        if (rc) free_observed();
+        return rc;
     }
 
     // ---------------------------------------------------------------- autotuner
@@ -2199,6 +2385,17 @@ int fwi_lbfgs_direction(void *ctx, int m, double *stats)
 {
     return ctx ? as_ctx(ctx)->lbfgs_direction(m, stats) : FWI_ERR_ARG;
 }
+int fwi_store_observed(void *ctx, const fwi_shot *shots, int n, const void *obs, int store_prec)
+{
+    return ctx ? as_ctx(ctx)->store_observed(shots, n, obs, store_prec) : FWI_ERR_ARG;
+}
+int fwi_model_observed(void *ctx, const fwi_shot *shots, int n, const void *v_hor, const void *v_po,
+                       const void *v_nmo, int store_prec)
+{
+    return ctx ? as_ctx(ctx)->model_observed(shots, n, v_hor, v_po, v_nmo, store_prec) : FWI_ERR_ARG;
+}
+int fwi_free_observed(void *ctx) { return ctx ? as_ctx(ctx)->free_observed() : FWI_ERR_ARG; }
+
 int fwi_set_lbfgs_guard(void *ctx, int on)
 {
     if (!ctx) return FWI_ERR_ARG;

@@ -138,6 +138,9 @@ def lib() -> C.CDLL:
                                      _p, _p])
         _sig(L, "fwi_direction_slope", [_p, _p])
         _sig(L, "fwi_set_lbfgs_guard", [_p, _i])
+        _sig(L, "fwi_store_observed", [_p, shotp, _i, _p, _i])
+        _sig(L, "fwi_model_observed", [_p, shotp, _i, _p, _p, _p, _i])
+        _sig(L, "fwi_free_observed", [_p])
         _sig(L, "fwi_load_model_files", [_p, C.c_char_p, C.c_char_p, C.c_char_p])
         _sig(L, "fwi_save_model_files", [_p, C.c_char_p, C.c_char_p, C.c_char_p])
         _sig(L, "fwi_set_frequency", [_p, _f, _i])
@@ -300,7 +303,7 @@ class Context:
             else:
                 setattr(o, k, v)
         self._inputs(shots, obs, mask)
-        hist = np.zeros(o.iterations, np.float64)
+        hist = np.zeros(o.iterations, np.float64)  # obs None: the records kept on the device
         done = C.c_int(0)
         _check(lib().fwi_invert(self._h, shots, len(shots), ptr(obs), ptr(mask), C.byref(o),
                                 hist.ctypes.data, C.byref(done)), "fwi_invert")
@@ -379,7 +382,8 @@ class Context:
         return (J.value, *out)
 
     def _inputs(self, shots, obs, mask):
-        _checked(obs, self.dtype, sum(s.nt * s.nrec for s in shots), "obs")
+        if obs is not None:  # None: the records kept on the device (store_observed / model_observed)
+            _checked(obs, self.dtype, sum(s.nt * s.nrec for s in shots), "obs")
         if mask is not None:
             _checked(mask, np.uint8, sum(s.nrec for s in shots), "mask")
 
@@ -389,6 +393,20 @@ class Context:
         _check(lib().fwi_misfit(self._h, shots, len(shots), ptr(obs), ptr(mask), C.byref(J)),
                "fwi_misfit")
         return J.value
+
+    def store_observed(self, shots, obs, store_prec=0):
+        """Keep these shots' records on the device (FP32, or FP16 with per-trace scales)."""
+        self._inputs(shots, obs, None)
+        _check(lib().fwi_store_observed(self._h, shots, len(shots), ptr(obs), int(store_prec)), "fwi_store_observed")
+
+    def model_observed(self, shots, vh, vp, vn, store_prec=0):
+        """Model these shots' records on the device from (vh, vp, vn) into the store."""
+        vh, vp, vn = self._grid(vh, vp, vn)
+        _check(lib().fwi_model_observed(self._h, shots, len(shots), ptr(vh), ptr(vp), ptr(vn), int(store_prec)),
+               "fwi_model_observed")
+
+    def free_observed(self):
+        _check(lib().fwi_free_observed(self._h), "fwi_free_observed")
 
     def set_gradient(self, gh, gp, gn):
         gh, gp, gn = self._grid(gh, gp, gn, what="gradient")

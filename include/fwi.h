@@ -126,11 +126,29 @@ int fwi_forward(void *ctx, const fwi_shot *shots, int nshots, void *traces);
 /* Misfit J = 1/2 sum mask (d - obs)^2 (FP64) and, with gradients requested,
  * dJ/dv_hor, dJ/dv_po, dJ/dv_nmo summed over the shots, [nz][nx] each
  * (src/main.c:408-534 with the MPI reduction replaced by an on-device sum).
- * obs: per shot [nt][nrec], concatenated.  mask: per shot [nrec] bytes
+ * obs: per shot [nt][nrec], concatenated; NULL: the records kept on the device (below).  mask: per shot [nrec] bytes
  * (0 = dropped trace), concatenated, or NULL.  g_* may be NULL (the gradient
  * then stays in the context for the L-BFGS calls below). */
 int fwi_gradient(void *ctx, const fwi_shot *shots, int nshots, const void *obs,
                  const unsigned char *mask, void *g_vh, void *g_vp, void *g_vn, double *misfit);
+
+/* ---- observed data kept on the device ----
+ * The reference re-models its observed data from the true model for every frequency band
+ * (src/main.c:321-366) and keeps the records of all shots in device memory (shot1,
+ * src/main.c:168).  fwi_store_observed copies given records (host or device, laid out as
+ * fwi_gradient takes them) into a store inside the context; fwi_model_observed models them
+ * there from the given model (squared velocities [nz][nx]) with fwi_forward's arithmetic, without
+ * a host copy, and keeps the context's own model.  store_prec FWI_SPREC_NATIVE keeps the records
+ * as they are (4 B per sample in FP32 contexts: 65.5 GB for 512 shots of 8000 x 4001); FWI_SPREC_FP16
+ * keeps 2 B per sample with one scale per trace (max |d| / 32768), a relative error of about 2^-12
+ * of each trace's largest value.  Later fwi_gradient / fwi_misfit calls (and fwi_invert,
+ * fwi_invert_bands) with obs == NULL on the same shots, in the same order, read the store
+ * (FWI_ERR_ARG for other shots).  fwi_free_observed releases it.  No counterpart in the reference's
+ * call surface. */
+int fwi_store_observed(void *ctx, const fwi_shot *shots, int nshots, const void *obs, int store_prec);
+int fwi_model_observed(void *ctx, const fwi_shot *shots, int nshots, const void *v_hor, const void *v_po,
+                       const void *v_nmo, int store_prec);
+int fwi_free_observed(void *ctx);
 
 /* Misfit only (forward + residual), e.g. for line-search trials (src/main.c:695-737). */
 int fwi_misfit(void *ctx, const fwi_shot *shots, int nshots, const void *obs,
@@ -208,7 +226,9 @@ int fwi_set_frequency(void *ctx, float f, int nt);
 /* Multiscale inversion (src/main.c:274-806): band b at peak frequency f0 + b df
  * (the reference: f += 3).  Per band: fwi_set_frequency(f, nt); the band's observed data
  * from band_obs (the caller's records, or its own forward modelling with
- * fwi_forward), host or device, laid out as fwi_gradient takes them; then fwi_invert with
+ * fwi_forward), host or device, laid out as fwi_gradient takes them, or NULL when the
+ * callback left them in the context's store (fwi_model_observed: re-modelled on the device at
+ * the band's frequency); then fwi_invert with
  * alpha and the halving count starting afresh (src/main.c:308-311).  restart_model != 0
  * starts every band from the model the call began with, as the reference does (it
  * rebuilds the model from the initial Vp, eps, delta at src/main.c:318); 0 continues from
