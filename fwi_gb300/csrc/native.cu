@@ -818,9 +818,7 @@ template <typename T> struct Ctx : CtxBase {
         drop_sections();
         for (void *p : allocs) cudaFree(p);
         for (const TileListEntry &e : tile_lists) cudaFree(e.dev);
-        free_observed();
-        for (void *p : {(void *)ostore_tmp, (void *)model_keep[0], (void *)model_keep[1], (void *)model_keep[2]})
-            if (p) cudaFree(p);
+        free_observed();  // (the store's scratch and the kept model are among allocs)
         if (ss.side) cudaStreamSynchronize(ss.side);
         if (rst) cudaStreamSynchronize(rst);
         for (auto &e : ev)

@@ -59,7 +59,7 @@ def test_store_and_model_observed_equal_passed_records():
     assert g16m[0] == g16[0] and all(np.array_equal(a, b) for a, b in zip(g16m[1:], g16[1:]))
     # other shots than the stored ones, or no store at all, are refused
     with pytest.raises(FwiError):
-        ctx.gradient(shots[:1], None)
+        ctx.gradient(make_shots(exact_shots(p)[:1]), None)
     ctx.free_observed()
     with pytest.raises(FwiError):
         ctx.misfit(shots, None)
