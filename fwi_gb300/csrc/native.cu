@@ -1126,6 +1126,22 @@ template <typename T> struct Ctx : CtxBase {
         }
     }
 
+    // Whether a batch of windows nxm wide runs on the small-shot cluster path: FP32, exact
+    // adjoint, every step's images kept (the path has no checkpoint or boundary variant), the
+    // window fitting a cluster's shared memory, and FWI_CLUSTER not set to 0.  Cached per width.
+    mutable std::vector<std::pair<int, bool>> cluster_fit;
+    bool cluster_path(int nxm) const
+    {
+        if (!(sizeof(T) == 4 && use_tma && cfg.mode == FWI_MODE_EXACT && cfg.store == FWI_STORE_FULL)) return false;
+        if (const char *e = getenv("FWI_CLUSTER"))
+            if (atoi(e) == 0) return false;
+        for (const auto &c : cluster_fit)
+            if (c.first == nxm) return c.second;
+        const bool ok = fwi::cluster_shot_fits(nxm, nz);
+        cluster_fit.emplace_back(nxm, ok);
+        return ok;
+    }
+
     // Device copies of the compact tile lists (Batch::tiles), one per window width, grid
     // origin, layer width and role, made on first use and kept for the context's life (a
     // captured graph reads them).  Null (full grid) if the list cannot be made.
@@ -1456,8 +1472,16 @@ template <typename T> struct Ctx : CtxBase {
                 const int seg = g / ck_every;
                 return seg >= first_direct ? g - seg * ck_every + (seg & 1) * ck_every : -1;
             };
+            // small shots on chip: one cluster per shot, every step in one launch (prop_cluster.cuh)
+            const bool on_cluster = cluster_path(nxm);
             NvtxRange fwd_range("fwi forward steps");
-            rc = run_section(section_key(0), 0, nsamp, spts[0], [&]() -> int {
+            if constexpr (sizeof(T) == 4) {
+                if (on_cluster) {
+                    TRY(fwi::launch_cluster_forward(bf, nxm, ntb, want_grad, st));
+                    launches++;
+                }
+            }
+            rc = on_cluster ? FWI_OK : run_section(section_key(0), 0, nsamp, spts[0], [&]() -> int {
                 int cur = 0;
                 for (int g = 0; g < ntb; g++) {
                     if (ckpt && g % ck_every == 0 && g / ck_every < first_direct) {
@@ -1495,7 +1519,17 @@ template <typename T> struct Ctx : CtxBase {
             }
             if (traces)
                 TRY(cudaMemcpyAsync((T *)traces + off[b0], rec, nrec_elems * sizeof(T), cudaMemcpyDefault, st));
-            if (want_grad) {
+            if (want_grad && on_cluster) {
+                NvtxRange adj_range("fwi adjoint steps + imaging");
+                for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
+                if constexpr (sizeof(T) == 4) TRY(fwi::launch_cluster_adjoint(b, nxm, ntb, st));
+                // one gradient slot per shot
+                k_accumulate_gradient<T><<<eg((long)nx * nz), 256, 0, st>>>(grad[0], grad[1], grad[2], gs[0], gs[1],
+                                                                            gs[2], shots, nb, 1, nx, nz, mpitch, pitch,
+                                                                            slot);
+                TRY_LAUNCH();
+                launches += 2;
+            } else if (want_grad) {
                 NvtxRange adj_range("fwi adjoint steps + imaging");
                 rc = run_section(section_key(1), 1, nsamp, spts[1], [&]() -> int {
                     for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));

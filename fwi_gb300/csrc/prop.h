@@ -212,6 +212,15 @@ void launch_adjoint_step(const Batch<T> &b, int nx_max, int j, int ntb, int cur,
 // device (once per device); call before their first launch there.
 cudaError_t prepare_fp32_kernels();
 
+// Small shots resident on chip (prop_cluster.cuh): one thread-block cluster per
+// shot takes it through every step in one launch.  cluster_shot_fits: the
+// window nx wide on an nz-row grid fits the cluster's shared memory and
+// clusters of that size can run on the current device (FP32, exact adjoint,
+// full image storage).  The launches cover every shot of the batch view.
+bool cluster_shot_fits(int nx_max, int nz);
+cudaError_t launch_cluster_forward(const Batch<float> &b, int nx_max, int ntb, bool images, cudaStream_t st);
+cudaError_t launch_cluster_adjoint(const Batch<float> &b, int nx_max, int ntb, cudaStream_t st);
+
 // Boundary storage (prop_boundary.cuh): ring length per shot, saving the
 // ring of step g, and the backward rebuild of the CPML-free region.
 long boundary_ring_len(int nx_max, int nz, int cpml);

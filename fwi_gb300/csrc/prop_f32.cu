@@ -9,6 +9,7 @@
 #include <mutex>
 
 #include "prop_boundary.cuh"
+#include "prop_cluster.cuh"
 #include "prop_layer.cuh"
 #include "prop_rebuild.cuh"
 
@@ -213,6 +214,106 @@ void launch_adjoint_step<float>(const Batch<float> &b, int nx_max, int j, int nt
 }
 
 long boundary_ring_len(int nx_max, int nz, int cpml) { return Ring::make(nx_max, nz, cpml).count(); }
+
+// ------------------------------------------------------------------ small shots on one cluster
+
+namespace {
+
+template <typename K> cudaError_t cluster_attrs(K kernel, size_t smem)
+{
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+// One cluster of kClusterCtas CTAs per shot; `args` are the kernel's own.
+template <typename... Args>
+cudaError_t cluster_launch(void (*kernel)(Args...), int nshots, size_t smem, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kClusterCtas * nshots);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+size_t cluster_smem_limit()
+{
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return (size_t)v - 1024;  // the kernels' static shared memory
+}
+
+}  // namespace
+
+bool cluster_shot_fits(int nx_max, int nz)
+{
+    ClusterPlan p;
+    if (!cluster_plan(nx_max, nz, cluster_smem_limit(), p)) return false;
+    for (cudaError_t e : {cluster_attrs(k_cluster_fwd<kStoreNative>, p.smem_fwd),
+                          cluster_attrs(k_cluster_fwd<kStoreHalf>, p.smem_fwd),
+                          cluster_attrs(k_cluster_fwd<kStoreBf16>, p.smem_fwd),
+                          cluster_attrs(k_cluster_adj<kStoreNative>, p.smem_adj),
+                          cluster_attrs(k_cluster_adj<kStoreHalf>, p.smem_adj),
+                          cluster_attrs(k_cluster_adj<kStoreBf16>, p.smem_adj)})
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+    // clusters of kClusterCtas CTAs with this much shared memory each must fit on the device
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = p.smem_adj;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_cluster_adj<kStoreHalf>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n > 0;
+}
+
+cudaError_t launch_cluster_forward(const Batch<float> &b, int nx_max, int ntb, bool images, cudaStream_t st)
+{
+    ClusterPlan p;
+    if (!cluster_plan(nx_max, b.nz, cluster_smem_limit(), p)) return cudaErrorInvalidValue;
+    const int img = images ? 1 : 0;
+    switch (b.store_type) {
+    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
+    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
+    default: return cluster_launch(k_cluster_fwd<kStoreNative>, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
+    }
+}
+
+cudaError_t launch_cluster_adjoint(const Batch<float> &b, int nx_max, int ntb, cudaStream_t st)
+{
+    ClusterPlan p;
+    if (!cluster_plan(nx_max, b.nz, cluster_smem_limit(), p)) return cudaErrorInvalidValue;
+    switch (b.store_type) {
+    case kStoreHalf: return cluster_launch(k_cluster_adj<kStoreHalf>, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
+    case kStoreBf16: return cluster_launch(k_cluster_adj<kStoreBf16>, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
+    default: return cluster_launch(k_cluster_adj<kStoreNative>, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
+    }
+}
 
 template void launch_save_ring<float>(const Batch<float> &, int, int, int, int, float *, long, cudaStream_t);
 template void launch_rebuild_begin<float>(const Batch<float> &, int, int, int, int, const float *, long,
