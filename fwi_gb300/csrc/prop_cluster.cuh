@@ -4,27 +4,33 @@
 // A shot whose grid fits the cluster's shared memory (C1: 209 x 209) gains
 // nothing from the tile passes' per-step launches: one step of one small shot
 // is a few microseconds of work, less than the launch and dependency latency
-// of the two tile passes.  Here a cluster of kClusterCtas CTAs (16: a
-// non-portable cluster size, enabled per kernel) takes one shot through all
-// its time steps in a single launch.  CTA k owns the interior rows
-// [4 + k h, 4 + (k + 1) h) of the shot's window, every column, and keeps the
-// state of its rows in its own shared memory; the stencils read the 4 rows
-// beyond its own from the neighbouring CTAs' shared memory (distributed
-// shared memory, map_shared_rank), and the phases of a step are separated by
-// cluster barriers (barrier.cluster: hardware, with release / acquire
-// semantics over the cluster's shared memory).  No other wait exists, and
+// of the two tile passes.  Here a cluster of up to 16 CTAs (a non-portable
+// cluster size, enabled per kernel) takes one shot through all its time steps
+// in a single launch.  CTA k owns the interior rows [4 + k h, 4 + (k + 1) h)
+// of the shot's window (h >= 8), every column, and keeps the state of its rows
+// in its own shared memory.  After each step's cluster barrier (barrier.cluster:
+// hardware, release / acquire over the cluster's shared memory) it copies the
+// 8 rows above and below its own of the one field the next step's z-stencils
+// need from the neighbours' shared memory (distributed shared memory) and
+// recomputes the CPML auxiliary field of the 4 rows either side itself, so
+// that a step needs a single cluster barrier.  No other wait exists, and
 // every thread of every CTA runs the same number of steps and barriers.
 //
-// Forward step (2 barriers): psi of the band points from the current level;
-// barrier; everything else (zeta, the increment update, the next level into
-// the other half of a ping-pong pair, receivers, images) and the CTA's max of
-// |P|, |F|; barrier; every CTA reads all CTAs' maxima (the next step's image
-// scale).  Exact adjoint step (3 barriers): g, h, Z and the fields u of the
-// Laplacian terms; barrier; Y of the band points from the neighbours' u;
-// barrier; the increment and lambda update, residual injection and imaging;
-// barrier.  The arithmetic is the tile passes' (difference-form Laplacian,
-// increment-form leapfrog, the same CPML recursions), evaluated in another
-// order: results agree with them to FP32 rounding.
+// Forward step: copy the 8-row halo of F; psi_x of the band points of the own
+// rows, psi_z of the band points of the own rows and 4 either side; zeta, the
+// increment update, the next level into the other half of a ping-pong pair,
+// receivers, images and the CTA's max of |P|, |F|; barrier; every CTA reads
+// all CTAs' maxima (the next step's image scale).  Exact adjoint step: copy
+// the 8-row halo of u_z; Y_x of the own band points, Y_z of the band points of
+// the own rows and 4 either side; the increment and lambda update, residual
+// injection, imaging, and then at once the next step's g, h, Z and fields u
+// from the new lambda (into the other half of a ping-pong pair); barrier.
+// Both fields the halos come from are double-buffered, so a neighbour's copy
+// of step t and the owner's writes of step t + 1 never meet.  The arithmetic
+// is the tile passes' (difference-form Laplacian, increment-form leapfrog, the
+// same CPML recursions), evaluated in another order: results agree with them
+// to FP32 rounding; the recomputed halo values are bit-identical to the
+// owner's (same inputs, same operations).
 #pragma once
 
 #include <cooperative_groups.h>
@@ -35,97 +41,143 @@ namespace fwi {
 
 namespace cg = cooperative_groups;
 
-constexpr int kClusterCtas = 16;
+constexpr int kClusterMaxCtas = 16;
 constexpr int kClusterThreads = 1024;
-constexpr int kClusterFwdArrays = 13;  // P0 P1 F0 F1 PSX PSZ VP VF ZX ZZ MH MP MN
-constexpr int kClusterAdjArrays = 16;  // LP LF WP WF UX UZ ZX ZZ YX YZ MH MP MN GH GP GN
+constexpr int kClHalo = 2 * kRad;  // halo rows of the copied fields
 
-// Rows per CTA and shared-memory row pitch of a window nx wide on an nz-row grid.
+// CTAs, rows per CTA and shared-memory row pitch of a window nx wide on an nz-row grid.
+// Shared arrays: "haloed" ones carry kClHalo rows above and below the own rows, "banded" ones
+// kRad rows (the recomputed CPML fields), the rest only the own rows; the CPML coefficients sit
+// in shared tables by column and by banded row.
 struct ClusterPlan {
-    int h = 0, pitch = 0;
+    int ncta = 0, h = 0, pitch = 0;
     size_t smem_fwd = 0, smem_adj = 0;
 };
+
+// forward: F0 F1 haloed; PSZ banded; P0 P1 PSX VP VF ZX ZZ MH MP MN own
+// adjoint: UZ0 UZ1 haloed; YZ banded; LP LF WP WF UX0 UX1 ZX ZZ YX GH GP GN own (the model
+// coefficients read through the read-only cache)
+constexpr int kClFwdHaloed = 2, kClFwdOwn = 10;
+constexpr int kClAdjHaloed = 2, kClAdjOwn = 12;
+
+inline size_t cluster_smem(int h, int pitch, int haloed, int own)
+{
+    const size_t rows = (size_t)haloed * (h + 2 * kClHalo) + (h + 2 * kRad) + (size_t)own * h;
+    return sizeof(float) * (rows * pitch + 2 * (size_t)pitch + 2 * (size_t)(h + 2 * kRad)) + 64;
+}
 
 inline bool cluster_plan(int nx, int nz, size_t smem_limit, ClusterPlan &p)
 {
     const int nzi = nz - 8;
-    if (nzi <= 0 || nx < 9) return false;
-    p.h = (nzi + kClusterCtas - 1) / kClusterCtas;
+    if (nzi < kClHalo || nx < 9) return false;
+    // a halo comes from one neighbour only: h >= 8
+    p.ncta = nzi / kClHalo < kClusterMaxCtas ? nzi / kClHalo : kClusterMaxCtas;
+    p.h = (nzi + p.ncta - 1) / p.ncta;
     p.pitch = (nx + 3) / 4 * 4;
-    p.smem_fwd = sizeof(float) * (size_t)kClusterFwdArrays * p.h * p.pitch + 64;
-    p.smem_adj = sizeof(float) * (size_t)kClusterAdjArrays * p.h * p.pitch + 64;
-    // the z-stencils reach 4 rows: one neighbour on either side
-    return p.h >= kRad && p.smem_adj <= smem_limit && p.smem_fwd <= smem_limit;
+    p.smem_fwd = cluster_smem(p.h, p.pitch, kClFwdHaloed, kClFwdOwn);
+    p.smem_adj = cluster_smem(p.h, p.pitch, kClAdjHaloed, kClAdjOwn);
+    return p.smem_adj <= smem_limit && p.smem_fwd <= smem_limit;
 }
 
-// Rows of one shared array: this CTA's own, and the neighbours' above and below.
-struct ClRows {
-    float *own;
-    const float *up, *down;
-    int h, pitch, k, nz;
-    // value at own-relative row lr (-4 .. h + 3), column ix; zero on the frame rows
-    __device__ __forceinline__ float at(int lr, int ix) const
+// Geometry of one CTA's rows and the thread's walk over its points: point q = threadIdx.x +
+// n blockDim.x of the own rows x interior columns, stepped by carries instead of divisions.
+struct ClGeom {
+    int k, ncta, h, pitch, nx, nz, iz0, nrows, nxi, npts;
+    int dlr, dix;  // blockDim.x = dlr rows + dix columns
+    __device__ void init(int k_, int ncta_, int h_, int pitch_, int nx_, int nz_)
     {
-        const int iz = 4 + k * h + lr;
-        if (iz < 4 || iz >= nz - 4) return 0.f;
-        if (lr < 0) return up[(lr + h) * pitch + ix];
-        if (lr >= h) return down[(lr - h) * pitch + ix];
-        return own[lr * pitch + ix];
+        k = k_;
+        ncta = ncta_;
+        h = h_;
+        pitch = pitch_;
+        nx = nx_;
+        nz = nz_;
+        iz0 = 4 + k * h;
+        nrows = max(0, min(h, nz - 4 - iz0));
+        nxi = nx - 8;
+        npts = nrows * nxi;
+        dlr = (int)blockDim.x / nxi;
+        dix = (int)blockDim.x - dlr * nxi;
     }
 };
 
-__device__ __forceinline__ ClRows cl_rows(cg::cluster_group &cl, float *own, int h, int pitch, int k, int ncta, int nz)
+// Each thread's walk: for (ClWalk w(g); w.on(); w.next()) { w.lr, w.ix }
+struct ClWalk {
+    int q, lr, ix;
+    const ClGeom &g;
+    __device__ explicit ClWalk(const ClGeom &g_) : g(g_)
+    {
+        q = threadIdx.x;
+        lr = q / g.nxi;
+        ix = 4 + q - lr * g.nxi;
+    }
+    __device__ bool on() const { return q < g.npts; }
+    __device__ void next()
+    {
+        q += blockDim.x;
+        lr += g.dlr;
+        ix += g.dix;
+        if (ix >= g.nx - 4) {
+            ix -= g.nxi;
+            lr++;
+        }
+    }
+};
+
+// The kClHalo rows above and below the CTA's own of a haloed array (own row r at row
+// r + kClHalo) from the neighbours' own rows after a cluster barrier; frame rows read zero.
+__device__ __forceinline__ void cl_fill_halo(cg::cluster_group &cl, const ClGeom &g, float *a)
 {
-    ClRows r;
-    r.own = own;
-    r.up = k > 0 ? cl.map_shared_rank(own, k - 1) : own;
-    r.down = k + 1 < ncta ? cl.map_shared_rank(own, k + 1) : own;
-    r.h = h;
-    r.pitch = pitch;
-    r.k = k;
-    r.nz = nz;
-    return r;
+    const int p4 = g.pitch / 4, n = 2 * kClHalo * p4;
+    const float4 *up = g.k > 0 ? reinterpret_cast<const float4 *>(cl.map_shared_rank(a, g.k - 1)) : nullptr;
+    const float4 *down = g.k + 1 < g.ncta ? reinterpret_cast<const float4 *>(cl.map_shared_rank(a, g.k + 1)) : nullptr;
+    float4 *a4 = reinterpret_cast<float4 *>(a);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int hr = e / p4, c = e - hr * p4;
+        if (hr < kClHalo) {  // global row iz0 - 8 + hr: the upper neighbour's own row h - 8 + hr
+            const int iz = g.iz0 - kClHalo + hr;
+            a4[hr * p4 + c] = (iz >= 4 && up) ? up[(g.h + hr) * p4 + c] : z;
+        } else {  // global row iz0 + h + hr - 8: the lower neighbour's own row hr - 8
+            const int iz = g.iz0 + g.h + hr - kClHalo;
+            a4[(g.h + hr) * p4 + c] = (iz < g.nz - 4 && down) ? down[hr * p4 + c] : z;
+        }
+    }
 }
 
-// 8th-order derivatives (unnormalised) at (lr, ix): along x from the CTA's own row, along z
-// through ClRows.  Difference form for the second derivative, as the tile passes.
-__device__ __forceinline__ float cl_d2x(const float *row, int ix)
+// 8th-order derivatives (unnormalised) at c along stride st (1: x, the pitch: z).  Difference
+// form for the second derivative, as the tile passes.
+__device__ __forceinline__ float cl_d2(const float *c, int st)
 {
     using C = Coef<float>;
-    const float o = row[ix];
-    return C::d2_1 * ((row[ix + 1] - o) + (row[ix - 1] - o)) - C::d2_2 * ((row[ix + 2] - o) + (row[ix - 2] - o)) +
-           C::d2_3 * ((row[ix + 3] - o) + (row[ix - 3] - o)) - C::d2_4 * ((row[ix + 4] - o) + (row[ix - 4] - o));
+    const float o = c[0];
+    return C::d2_1 * ((c[st] - o) + (c[-st] - o)) - C::d2_2 * ((c[2 * st] - o) + (c[-2 * st] - o)) +
+           C::d2_3 * ((c[3 * st] - o) + (c[-3 * st] - o)) - C::d2_4 * ((c[4 * st] - o) + (c[-4 * st] - o));
 }
-__device__ __forceinline__ float cl_d1x(const float *row, int ix)
+__device__ __forceinline__ float cl_d1(const float *c, int st)
 {
     using C = Coef<float>;
-    return C::d1_1 * (row[ix + 1] - row[ix - 1]) - C::d1_2 * (row[ix + 2] - row[ix - 2]) +
-           C::d1_3 * (row[ix + 3] - row[ix - 3]) - C::d1_4 * (row[ix + 4] - row[ix - 4]);
-}
-__device__ __forceinline__ float cl_d2z(const ClRows &a, int lr, int ix)
-{
-    using C = Coef<float>;
-    const float o = a.at(lr, ix);
-    return C::d2_1 * ((a.at(lr + 1, ix) - o) + (a.at(lr - 1, ix) - o)) -
-           C::d2_2 * ((a.at(lr + 2, ix) - o) + (a.at(lr - 2, ix) - o)) +
-           C::d2_3 * ((a.at(lr + 3, ix) - o) + (a.at(lr - 3, ix) - o)) -
-           C::d2_4 * ((a.at(lr + 4, ix) - o) + (a.at(lr - 4, ix) - o));
-}
-__device__ __forceinline__ float cl_d1z(const ClRows &a, int lr, int ix)
-{
-    using C = Coef<float>;
-    return C::d1_1 * (a.at(lr + 1, ix) - a.at(lr - 1, ix)) - C::d1_2 * (a.at(lr + 2, ix) - a.at(lr - 2, ix)) +
-           C::d1_3 * (a.at(lr + 3, ix) - a.at(lr - 3, ix)) - C::d1_4 * (a.at(lr + 4, ix) - a.at(lr - 4, ix));
+    return C::d1_1 * (c[st] - c[-st]) - C::d1_2 * (c[2 * st] - c[-2 * st]) + C::d1_3 * (c[3 * st] - c[-3 * st]) -
+           C::d1_4 * (c[4 * st] - c[-4 * st]);
 }
 
-// CPML coefficient of column ix / row iz of an nx x nz window (0 outside the layers).
-__device__ __forceinline__ float cl_coef_x(const float *tab, int ix, int nx, int cpml)
+// CPML coefficient tables of the CTA: by column (0 outside the side layers) and by banded row
+// (row r of the table: global row iz0 - 4 + r; 0 outside the bottom layer).
+__device__ __forceinline__ void cl_tables(const Batch<float> &b, const ClGeom &g, float *ax, float *bx, float *az,
+                                          float *bz)
 {
-    return ix < cpml ? tab[cpml - ix] : ix > nx - cpml - 1 ? tab[ix - nx + cpml + 1] : 0.f;
-}
-__device__ __forceinline__ float cl_coef_z(const float *tab, int iz, int nz, int cpml)
-{
-    return iz > nz - cpml - 1 ? tab[iz - nz + cpml + 1] : 0.f;
+    const int cp = b.cpml;
+    for (int ix = threadIdx.x; ix < g.pitch; ix += blockDim.x) {
+        const int d = ix >= g.nx ? 0 : ix < cp ? cp - ix : ix > g.nx - cp - 1 ? ix - g.nx + cp + 1 : 0;
+        ax[ix] = d ? b.cpa[d] : 0.f;
+        bx[ix] = d ? b.cpb[d] : 0.f;
+    }
+    for (int r = threadIdx.x; r < g.h + 2 * kRad; r += blockDim.x) {
+        const int iz = g.iz0 - kRad + r;
+        const int d = (iz > g.nz - cp - 1 && iz < g.nz) ? iz - g.nz + cp + 1 : 0;
+        az[r] = d ? b.cpa[d] : 0.f;
+        bz[r] = d ? b.cpb[d] : 0.f;
+    }
 }
 
 // Max over the CTA into *slot (values >= 0).
@@ -142,8 +194,20 @@ __device__ __forceinline__ void cl_block_max(float v, float *slot)
     }
 }
 
-// Forward of shot blockIdx.x / kClusterCtas of the batch through all its steps (global steps
-// ntb - nt .. ntb - 1); every step's images (img != 0) to slot g of the image store.
+// The banded rows of the CTA in z-band (bottom layer) that lie inside the interior: rows
+// r in [-4, h + 4) with global row iz0 + r in [max(4, zb), nz - 4); walked as r0 + q / nxi.
+struct ClBand {
+    int r0, npts;
+    __device__ ClBand(const ClGeom &g, int zb)
+    {
+        const int lo = max(max(4, zb), g.iz0 - kRad), hi = min(g.nz - 4, g.iz0 + g.h + kRad);
+        r0 = lo - g.iz0;
+        npts = hi > lo ? (hi - lo) * g.nxi : 0;
+    }
+};
+
+// Forward of shot blockIdx.x / ncta of the batch through all its steps (global steps ntb - nt
+// .. ntb - 1); every step's images (img != 0) to slot g of the image store.
 template <int ST>
 __global__ void __launch_bounds__(kClusterThreads, 1)
 k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
@@ -151,35 +215,39 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
     using Cd = Codec<float, ST>;
     using SI = typename Cd::S;
     extern __shared__ __align__(16) float csm[];
-    __shared__ float s_max;
+    __shared__ float s_max[2];
     cg::cluster_group cl = cg::this_cluster();
-    const int k = (int)cl.block_rank(), ncta = (int)cl.num_blocks();
+    const int ncta = (int)cl.num_blocks();
     const int s = blockIdx.x / ncta;
     const DevShot sh = b.shots[s];
+    ClGeom G;
+    G.init((int)cl.block_rank(), ncta, h, pitch, sh.nx, b.nz);
     const int nx = sh.nx, nz = b.nz, cpml = b.cpml;
-    const size_t plane = (size_t)h * pitch;
-    float *const P0 = csm, *const P1 = csm + plane, *const F0 = csm + 2 * plane, *const F1 = csm + 3 * plane;
-    float *PSX = csm + 4 * plane, *PSZ = csm + 5 * plane, *VP = csm + 6 * plane, *VF = csm + 7 * plane;
-    float *ZX = csm + 8 * plane, *ZZ = csm + 9 * plane, *MH = csm + 10 * plane, *MP = csm + 11 * plane,
-          *MN = csm + 12 * plane;
-    const int iz0 = 4 + k * h;
-    const int nrows = max(0, min(h, nz - 4 - iz0));  // own interior rows
-    const int nxi = nx - 8, npts = nrows * nxi;
-    for (size_t i = threadIdx.x; i < (size_t)kClusterFwdArrays * plane; i += blockDim.x) csm[i] = 0.f;
+    const size_t hp = (size_t)(h + 2 * kClHalo) * pitch, bp = (size_t)(h + 2 * kRad) * pitch,
+                 op = (size_t)h * pitch;
+    float *const F0 = csm, *const F1 = csm + hp, *const PSZ = csm + 2 * hp;
+    float *const base = PSZ + bp;
+    float *const P0 = base, *const P1 = base + op, *const PSX = base + 2 * op, *const VP = base + 3 * op,
+                 *const VF = base + 4 * op, *const ZX = base + 5 * op, *const ZZ = base + 6 * op,
+                 *const MH = base + 7 * op, *const MP = base + 8 * op, *const MN = base + 9 * op;
+    float *const AX = base + 10 * op, *const BX = AX + pitch, *const AZ = BX + pitch, *const BZ = AZ + h + 2 * kRad;
+    const size_t total = 2 * hp + bp + 10 * op;
+    for (size_t i = threadIdx.x; i < total; i += blockDim.x) csm[i] = 0.f;
+    cl_tables(b, G, AX, BX, AZ, BZ);
     __syncthreads();
-    for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-        const int lr = q / nxi, ix = 4 + q - lr * nxi;
-        const long mi = (long)(iz0 + lr) * b.mpitch + sh.x0 + ix;
-        MH[lr * pitch + ix] = b.mh[mi];
-        MP[lr * pitch + ix] = b.mp[mi];
-        MN[lr * pitch + ix] = b.mn[mi];
+    for (ClWalk w(G); w.on(); w.next()) {
+        const long mi = (long)(G.iz0 + w.lr) * b.mpitch + sh.x0 + w.ix;
+        const int i = w.lr * pitch + w.ix;
+        MH[i] = b.mh[mi];
+        MP[i] = b.mp[mi];
+        MN[i] = b.mn[mi];
     }
-    if (threadIdx.x == 0) s_max = 0.f;
     cl.sync();  // every CTA's state zeroed before any neighbour reads it
-    const ClRows fz0 = cl_rows(cl, F0, h, pitch, k, ncta, nz), fz1 = cl_rows(cl, F1, h, pitch, k, ncta, nz);
-    const ClRows psz = cl_rows(cl, PSZ, h, pitch, k, ncta, nz);
     const float inv_dh = b.inv_dh, inv_dh2 = b.inv_dh2;
     const int nrec = sh.rx1 - sh.rx0;
+    const int zb = nz - cpml;  // first row of the bottom layer
+    const ClBand band(G, zb);
+    const int nbx = cpml > 4 ? min(2 * (cpml - 4), G.nxi) : 0;  // side-band columns of a row
     float amax = 0.f;  // max |P|, |F| after the previous step, over the shot
     int cur = 0;
     for (int it = 0; it < sh.nt; it++) {
@@ -187,80 +255,85 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
         // the current level and the next (selected, not indexed: no local-memory arrays)
         float *const Pc = cur ? P1 : P0, *const Fc = cur ? F1 : F0;
         float *const Pn = cur ? P0 : P1, *const Fn = cur ? F0 : F1;
-        const ClRows fzc = cur ? fz1 : fz0;
-        // psi of the band points from the current level (src/parallelcalls.cu:48-63)
-        for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-            const int lr = q / nxi, ix = 4 + q - lr * nxi, iz = iz0 + lr, i = lr * pitch + ix;
-            if (!layer_point(ix, iz, nx, nz, cpml)) continue;
-            if (ix < cpml || ix > nx - cpml - 1)
-                PSX[i] = cl_coef_x(b.cpb, ix, nx, cpml) * PSX[i] +
-                         cl_coef_x(b.cpa, ix, nx, cpml) * (cl_d1x(Pc + lr * pitch, ix) * inv_dh);
-            if (iz > nz - cpml - 1)
-                PSZ[i] = cl_coef_z(b.cpb, iz, nz, cpml) * PSZ[i] +
-                         cl_coef_z(b.cpa, iz, nz, cpml) * (cl_d1z(fzc, lr, ix) * inv_dh);
+        cl_fill_halo(cl, G, Fc);
+        __syncthreads();
+        // psi (src/parallelcalls.cu:48-63): x of the side-band points of the own rows ...
+        for (int q = threadIdx.x; q < G.nrows * nbx; q += blockDim.x) {
+            const int lr = q / nbx, c = q - lr * nbx;
+            const int ix = c < nbx / 2 ? 4 + c : nx - 4 - nbx + c;
+            const int i = lr * pitch + ix;
+            PSX[i] = BX[ix] * PSX[i] + AX[ix] * (cl_d1(Pc + i, 1) * inv_dh);
         }
-        cl.sync();
+        // ... z of the bottom-band points of the own rows and 4 either side
+        for (int q = threadIdx.x; q < band.npts; q += blockDim.x) {
+            const int rr = q / G.nxi, r = band.r0 + rr, ix = 4 + q - rr * G.nxi;
+            const int ib = (r + kRad) * pitch + ix, ih = (r + kClHalo) * pitch + ix;
+            PSZ[ib] = BZ[r + kRad] * PSZ[ib] + AZ[r + kRad] * (cl_d1(Fc + ih, pitch) * inv_dh);
+        }
+        __syncthreads();
         const float sc = Cd::scaled ? image_scale(amax, inv_dh2) : 1.f;
-        if (img && Cd::scaled && k == 0 && threadIdx.x == 0) b.scale[(long)s * b.nt_max + g] = sc;
-        const float w = b.wavelet[it];
+        if (img && Cd::scaled && G.k == 0 && threadIdx.x == 0) b.scale[(long)s * b.nt_max + g] = sc;
+        const float wv = b.wavelet[it];
         SI *imgp = img ? (SI *)b.store + ((long)s * b.n_img + g) * 2 * b.slot : nullptr;
         float lmax = 0.f;
         bool sat = false;
-        for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-            const int lr = q / nxi, ix = 4 + q - lr * nxi, iz = iz0 + lr, i = lr * pitch + ix;
-            const float *prow = Pc + lr * pitch;
-            const float gP = cl_d2x(prow, ix) * inv_dh2, gF = cl_d2z(fzc, lr, ix) * inv_dh2;
-            float G = gP, H = gF;
-            if (layer_point(ix, iz, nx, nz, cpml)) {
-                const float tx = cl_d1x(PSX + lr * pitch, ix) * inv_dh, tz = cl_d1z(psz, lr, ix) * inv_dh;
+        for (ClWalk w(G); w.on(); w.next()) {
+            const int ix = w.ix, iz = G.iz0 + w.lr, i = w.lr * pitch + ix, ih = (w.lr + kClHalo) * pitch + ix;
+            const float gP = cl_d2(Pc + i, 1) * inv_dh2, gF = cl_d2(Fc + ih, pitch) * inv_dh2;
+            float Gv = gP, Hv = gF;
+            const bool xl = ix < cpml || ix > nx - cpml - 1, zl = iz >= zb;
+            if (xl || zl) {
+                const int ib = (w.lr + kRad) * pitch + ix;
+                const float tx = cl_d1(PSX + i, 1) * inv_dh, tz = cl_d1(PSZ + ib, pitch) * inv_dh;
                 float nzx = 0.f, nzz = 0.f;
-                if (ix < cpml || ix > nx - cpml - 1) {
-                    nzx = cl_coef_x(b.cpb, ix, nx, cpml) * ZX[i] + cl_coef_x(b.cpa, ix, nx, cpml) * (gP + tx);
+                if (xl) {
+                    nzx = BX[ix] * ZX[i] + AX[ix] * (gP + tx);
                     ZX[i] = nzx;
                 }
-                if (iz > nz - cpml - 1) {
-                    nzz = cl_coef_z(b.cpb, iz, nz, cpml) * ZZ[i] + cl_coef_z(b.cpa, iz, nz, cpml) * (gF + tz);
+                if (zl) {
+                    nzz = BZ[w.lr + kRad] * ZZ[i] + AZ[w.lr + kRad] * (gF + tz);
                     ZZ[i] = nzz;
                 }
-                G = gP + (tx + nzx);
-                H = gF + (tz + nzz);
+                Gv = gP + (tx + nzx);
+                Hv = gF + (tz + nzz);
             }
-            const float mpH = MP[i] * H;
-            float vp = VP[i] + (MH[i] * G + mpH), vf = VF[i] + (MN[i] * G + mpH);
+            const float mpH = MP[i] * Hv;
+            float vp = VP[i] + (MH[i] * Gv + mpH), vf = VF[i] + (MN[i] * Gv + mpH);
             if (iz == sh.sz && ix == sh.sx) {
-                vp += w;
-                vf += w;
+                vp += wv;
+                vf += wv;
             }
             VP[i] = vp;
             VF[i] = vf;
-            const float nP = prow[ix] + vp, nF = Fc[i] + vf;
+            const float nP = Pc[i] + vp, nF = Fc[ih] + vf;
             Pn[i] = nP;
-            Fn[i] = nF;
+            Fn[ih] = nF;
             if (Cd::scaled) lmax = fmaxf(lmax, fmaxf(fabsf(nP), fabsf(nF)));
             if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1)
                 b.rec[sh.rec_off + (long)it * nrec + ix - sh.rx0] = nP + nF;
             if (img) {
                 const long o = (long)iz * b.pitch + ix;
-                imgp[o] = Cd::enc_flag(G, sc, sat);
-                imgp[b.slot + o] = Cd::enc_flag(H, sc, sat);
+                imgp[o] = Cd::enc_flag(Gv, sc, sat);
+                imgp[b.slot + o] = Cd::enc_flag(Hv, sc, sat);
             }
         }
         if (sat) atomicOr(b.status, kStatusSaturated);
-        if (Cd::scaled) cl_block_max(lmax, &s_max);
+        if (Cd::scaled) cl_block_max(lmax, &s_max[it & 1]);
         cl.sync();  // the new level, and every CTA's max, complete
         if (Cd::scaled) {
             float m = 0.f;
-            for (int r = 0; r < ncta; r++) m = fmaxf(m, *cl.map_shared_rank(&s_max, r));
+            for (int r = 0; r < G.ncta; r++) m = fmaxf(m, *cl.map_shared_rank(&s_max[it & 1], r));
             amax = m;
-            if (k == 0 && threadIdx.x == 0) b.amax[(long)s * (b.nt_max + 1) + g + 1] = m;
+            if (G.k == 0 && threadIdx.x == 0) b.amax[(long)s * (b.nt_max + 1) + g + 1] = m;
         }
         cur ^= 1;
     }
     cl.sync();  // no CTA leaves while a neighbour may still read its shared memory
 }
 
-// Exact adjoint of shot blockIdx.x / kClusterCtas with imaging from the image store (slot of
-// each global step), the residual in b.rec; the shot's gradient to its slot s of b.g.
+// Exact adjoint of shot blockIdx.x / ncta with imaging from the image store (slot of each
+// global step), the residual in b.rec; the shot's gradient accumulated into its slot s of b.g
+// (zeroed by the caller).
 template <int ST>
 __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float> b, int ntb, int h, int pitch)
 {
@@ -268,89 +341,97 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float>
     using SI = typename Cd::S;
     extern __shared__ __align__(16) float csm[];
     cg::cluster_group cl = cg::this_cluster();
-    const int k = (int)cl.block_rank(), ncta = (int)cl.num_blocks();
+    const int ncta = (int)cl.num_blocks();
     const int s = blockIdx.x / ncta;
     const DevShot sh = b.shots[s];
+    ClGeom G;
+    G.init((int)cl.block_rank(), ncta, h, pitch, sh.nx, b.nz);
     const int nx = sh.nx, nz = b.nz, cpml = b.cpml;
-    const size_t plane = (size_t)h * pitch;
-    float *LP = csm, *LF = csm + plane, *WP = csm + 2 * plane, *WF = csm + 3 * plane;
-    float *UX = csm + 4 * plane, *UZ = csm + 5 * plane, *ZX = csm + 6 * plane, *ZZ = csm + 7 * plane;
-    float *YX = csm + 8 * plane, *YZ = csm + 9 * plane, *MH = csm + 10 * plane, *MP = csm + 11 * plane,
-          *MN = csm + 12 * plane, *GH = csm + 13 * plane, *GP = csm + 14 * plane, *GN = csm + 15 * plane;
-    const int iz0 = 4 + k * h;
-    const int nrows = max(0, min(h, nz - 4 - iz0));
-    const int nxi = nx - 8, npts = nrows * nxi;
-    for (size_t i = threadIdx.x; i < (size_t)kClusterAdjArrays * plane; i += blockDim.x) csm[i] = 0.f;
-    __syncthreads();
-    for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-        const int lr = q / nxi, ix = 4 + q - lr * nxi;
-        const long mi = (long)(iz0 + lr) * b.mpitch + sh.x0 + ix;
-        MH[lr * pitch + ix] = b.mh[mi];
-        MP[lr * pitch + ix] = b.mp[mi];
-        MN[lr * pitch + ix] = b.mn[mi];
-    }
+    const size_t hp = (size_t)(h + 2 * kClHalo) * pitch, bp = (size_t)(h + 2 * kRad) * pitch,
+                 op = (size_t)h * pitch;
+    float *const UZ0 = csm, *const UZ1 = csm + hp, *const YZ = csm + 2 * hp;
+    float *const base = YZ + bp;
+    float *const LP = base, *const LF = base + op, *const WP = base + 2 * op, *const WF = base + 3 * op,
+                 *const UX0 = base + 4 * op, *const UX1 = base + 5 * op, *const ZX = base + 6 * op,
+                 *const ZZ = base + 7 * op, *const YX = base + 8 * op;
+    float *const AX = base + 9 * op, *const BX = AX + pitch, *const AZ = BX + pitch, *const BZ = AZ + h + 2 * kRad;
+    const size_t total = 2 * hp + bp + 9 * op;
+    for (size_t i = threadIdx.x; i < total; i += blockDim.x) csm[i] = 0.f;
+    cl_tables(b, G, AX, BX, AZ, BZ);
     cl.sync();
-    const ClRows uz = cl_rows(cl, UZ, h, pitch, k, ncta, nz), yz = cl_rows(cl, YZ, h, pitch, k, ncta, nz);
     const float inv_dh = b.inv_dh, inv_dh2 = b.inv_dh2, kk = b.img_scale;
     const int nrec = sh.rx1 - sh.rx0;
+    const int zb = nz - cpml;
+    const ClBand band(G, zb);
+    const int nbx = cpml > 4 ? min(2 * (cpml - 4), G.nxi) : 0;
+    float *const g0 = b.g[0] + (long)s * b.slot, *const g1 = b.g[1] + (long)s * b.slot,
+                 *const g2 = b.g[2] + (long)s * b.slot;
+    using C = Coef<float>;
+    // band membership of a point (x side layers or the bottom layer)
+    auto in_band = [&](int ix, int iz) { return ix < cpml || ix > nx - cpml - 1 || iz >= zb; };
+    int cur = 0;  // u of this step in UX0 / UZ0 (cur 0) or UX1 / UZ1; zero before the first step
     for (int j = 0; j < sh.nt; j++) {
         const int m = sh.nt - j;
         const int g_img = ntb - 1 - j;  // global step of the image this iteration pairs with
-        // g = dt^2 (v_hor lP + v_nmo lF), h = dt^2 v_po (lP + lF); Z and the fields u of the Laplacian terms
-        for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-            const int lr = q / nxi, ix = 4 + q - lr * nxi, iz = iz0 + lr, i = lr * pitch + ix;
-            const float lp = LP[i], lf = LF[i];
-            const float gx = MH[i] * lp + MN[i] * lf, hz = MP[i] * (lp + lf);
-            float ux = gx, uzv = hz;
-            if (layer_point(ix, iz, nx, nz, cpml)) {
-                const float zx = gx + cl_coef_x(b.cpb, ix, nx, cpml) * ZX[i];
-                const float zz = hz + cl_coef_z(b.cpb, iz, nz, cpml) * ZZ[i];
-                ZX[i] = zx;
-                ZZ[i] = zz;
-                ux = gx + cl_coef_x(b.cpa, ix, nx, cpml) * zx;
-                uzv = hz + cl_coef_z(b.cpa, iz, nz, cpml) * zz;
-            }
-            UX[i] = ux;
-            UZ[i] = uzv;
-        }
-        cl.sync();
-        // Y of the band points: Yx' = -Dx(wx) + bx Yx with wx = u at band points, 0 elsewhere
-        for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-            const int lr = q / nxi, ix = 4 + q - lr * nxi, iz = iz0 + lr, i = lr * pitch + ix;
-            if (!layer_point(ix, iz, nx, nz, cpml)) continue;
-            using C = Coef<float>;
+        float *const UXc = cur ? UX1 : UX0, *const UZc = cur ? UZ1 : UZ0;
+        float *const UXn = cur ? UX0 : UX1, *const UZn = cur ? UZ0 : UZ1;
+        cl_fill_halo(cl, G, UZc);
+        __syncthreads();
+        // Y of the band points: Y' = -D(w) + b Y with w = u at band points, 0 elsewhere; x of the
+        // side-band points of the own rows ...
+        for (int q = threadIdx.x; q < G.nrows * nbx; q += blockDim.x) {
+            const int lr = q / nbx, c = q - lr * nbx;
+            const int ix = c < nbx / 2 ? 4 + c : nx - 4 - nbx + c, iz = G.iz0 + lr;
+            const int i = lr * pitch + ix;
             auto wxv = [&](int dx) {
                 const int x2 = ix + dx;
-                return (x2 > 3 && x2 < nx - 4 && layer_point(x2, iz, nx, nz, cpml)) ? UX[lr * pitch + x2] : 0.f;
-            };
-            auto wzv = [&](int dz) {
-                const int z2 = iz + dz;
-                return (z2 > 3 && z2 < nz - 4 && layer_point(ix, z2, nx, nz, cpml)) ? uz.at(lr + dz, ix) : 0.f;
+                return (x2 > 3 && x2 < nx - 4 && in_band(x2, iz)) ? UXc[i + dx] : 0.f;
             };
             const float dwx = C::d1_1 * (wxv(1) - wxv(-1)) - C::d1_2 * (wxv(2) - wxv(-2)) +
                               C::d1_3 * (wxv(3) - wxv(-3)) - C::d1_4 * (wxv(4) - wxv(-4));
+            YX[i] = -(dwx * inv_dh) + BX[ix] * YX[i];
+        }
+        // ... z of the bottom-band points of the own rows and 4 either side
+        for (int q = threadIdx.x; q < band.npts; q += blockDim.x) {
+            const int rr = q / G.nxi, r = band.r0 + rr, ix = 4 + q - rr * G.nxi, iz = G.iz0 + r;
+            const int ib = (r + kRad) * pitch + ix, ih = (r + kClHalo) * pitch + ix;
+            auto wzv = [&](int dz) {
+                const int z2 = iz + dz;
+                return (z2 > 3 && z2 < nz - 4 && in_band(ix, z2)) ? UZc[ih + dz * pitch] : 0.f;
+            };
             const float dwz = C::d1_1 * (wzv(1) - wzv(-1)) - C::d1_2 * (wzv(2) - wzv(-2)) +
                               C::d1_3 * (wzv(3) - wzv(-3)) - C::d1_4 * (wzv(4) - wzv(-4));
-            YX[i] = -(dwx * inv_dh) + cl_coef_x(b.cpb, ix, nx, cpml) * YX[i];
-            YZ[i] = -(dwz * inv_dh) + cl_coef_z(b.cpb, iz, nz, cpml) * YZ[i];
+            YZ[ib] = -(dwz * inv_dh) + BZ[r + kRad] * YZ[ib];
         }
-        cl.sync();
-        // lambda^m: increments += Dxx(u) - Dx(a Y) (and z), residual at the receivers; imaging
+        __syncthreads();
+        // lambda^m: increments += Dxx(u) - Dx(a Y) (and z), residual at the receivers; imaging;
+        // then g, h, Z and u of the next step from the new lambda
         float inv_sc = 1.f;
         if (Cd::scaled) inv_sc = 1.f / b.scale[(long)s * b.nt_max + g_img];
         const SI *imgp = (const SI *)b.store + ((long)s * b.n_img + g_img) * 2 * b.slot;
-        for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-            const int lr = q / nxi, ix = 4 + q - lr * nxi, iz = iz0 + lr, i = lr * pitch + ix;
-            using C = Coef<float>;
-            const float *urow = UX + lr * pitch, *yrow = YX + lr * pitch;
-            auto vx = [&](int dx) { return cl_coef_x(b.cpa, ix + dx, nx, cpml) * yrow[ix + dx]; };
-            auto vz = [&](int dz) { return cl_coef_z(b.cpa, iz + dz, nz, cpml) * yz.at(lr + dz, ix); };
-            const float dvx = C::d1_1 * (vx(1) - vx(-1)) - C::d1_2 * (vx(2) - vx(-2)) + C::d1_3 * (vx(3) - vx(-3)) -
-                              C::d1_4 * (vx(4) - vx(-4));
-            const float dvz = C::d1_1 * (vz(1) - vz(-1)) - C::d1_2 * (vz(2) - vz(-2)) + C::d1_3 * (vz(3) - vz(-3)) -
-                              C::d1_4 * (vz(4) - vz(-4));
-            float wp = WP[i] + (cl_d2x(urow, ix) * inv_dh2 - dvx * inv_dh);
-            float wf = WF[i] + (cl_d2z(uz, lr, ix) * inv_dh2 - dvz * inv_dh);
+        for (ClWalk w(G); w.on(); w.next()) {
+            const int ix = w.ix, iz = G.iz0 + w.lr, i = w.lr * pitch + ix, ih = (w.lr + kClHalo) * pitch + ix;
+            const int rb = w.lr + kRad, ib = rb * pitch + ix;
+            const long o = (long)iz * b.pitch + ix;
+            const long mi = (long)iz * b.mpitch + sh.x0 + ix;
+            const float Gv = Cd::dec(imgp[o], inv_sc), Hv = Cd::dec(imgp[b.slot + o], inv_sc);
+            const float mh = __ldg(b.mh + mi), mp = __ldg(b.mp + mi), mn = __ldg(b.mn + mi);
+            const float gh = g0[o], gp = g1[o], gn = g2[o];
+            const float dxx = cl_d2(UXc + i, 1) * inv_dh2, dzz = cl_d2(UZc + ih, pitch) * inv_dh2;
+            float wp, wf;
+            if (ix < cpml + 4 || ix > nx - cpml - 5 || iz >= zb - 4) {  // a CPML coefficient within reach
+                auto vx = [&](int dx) { return AX[ix + dx] * YX[i + dx]; };
+                auto vz = [&](int dz) { return AZ[rb + dz] * YZ[ib + dz * pitch]; };
+                const float dvx = C::d1_1 * (vx(1) - vx(-1)) - C::d1_2 * (vx(2) - vx(-2)) +
+                                  C::d1_3 * (vx(3) - vx(-3)) - C::d1_4 * (vx(4) - vx(-4));
+                const float dvz = C::d1_1 * (vz(1) - vz(-1)) - C::d1_2 * (vz(2) - vz(-2)) +
+                                  C::d1_3 * (vz(3) - vz(-3)) - C::d1_4 * (vz(4) - vz(-4));
+                wp = WP[i] + (dxx - dvx * inv_dh);
+                wf = WF[i] + (dzz - dvz * inv_dh);
+            } else {
+                wp = WP[i] + dxx;
+                wf = WF[i] + dzz;
+            }
             if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1) {
                 const float d = b.rec[sh.rec_off + (long)(m - 1) * nrec + ix - sh.rx0];
                 wp += d;
@@ -361,22 +442,25 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float>
             const float lp = LP[i] + wp, lf = LF[i] + wf;
             LP[i] = lp;
             LF[i] = lf;
-            const long o = (long)iz * b.pitch + ix;
-            const float Gv = Cd::dec(imgp[o], inv_sc), Hv = Cd::dec(imgp[b.slot + o], inv_sc);
-            GH[i] += kk * Gv * lp;
-            GP[i] += kk * Hv * (lp + lf);
-            GN[i] += kk * Gv * lf;
+            g0[o] = gh + kk * Gv * lp;
+            g1[o] = gp + kk * Hv * (lp + lf);
+            g2[o] = gn + kk * Gv * lf;
+            // u of the next step: g = v_hor lP + v_nmo lF, h = v_po (lP + lF) (dt^2 folded in)
+            const float gx = mh * lp + mn * lf, hz = mp * (lp + lf);
+            float ux = gx, uzv = hz;
+            if (in_band(ix, iz)) {
+                const float zx = gx + BX[ix] * ZX[i];
+                const float zz = hz + BZ[rb] * ZZ[i];
+                ZX[i] = zx;
+                ZZ[i] = zz;
+                ux = gx + AX[ix] * zx;
+                uzv = hz + AZ[rb] * zz;
+            }
+            UXn[i] = ux;
+            UZn[ih] = uzv;
         }
-        cl.sync();  // u and Y of this step read by every neighbour before the next step rewrites them
-    }
-    // the shot's gradient to its own slot
-    const long so = (long)s * b.slot;
-    for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-        const int lr = q / nxi, ix = 4 + q - lr * nxi, iz = iz0 + lr, i = lr * pitch + ix;
-        const long o = so + (long)iz * b.pitch + ix;
-        b.g[0][o] = GH[i];
-        b.g[1][o] = GP[i];
-        b.g[2][o] = GN[i];
+        cl.sync();  // lambda and u of the next step complete in every CTA
+        cur ^= 1;
     }
 }
 

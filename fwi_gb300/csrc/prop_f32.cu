@@ -226,18 +226,19 @@ template <typename K> cudaError_t cluster_attrs(K kernel, size_t smem)
     return e;
 }
 
-// One cluster of kClusterCtas CTAs per shot; `args` are the kernel's own.
+// One cluster of ncta CTAs per shot; `args` are the kernel's own.
 template <typename... Args>
-cudaError_t cluster_launch(void (*kernel)(Args...), int nshots, size_t smem, cudaStream_t st, Args... args)
+cudaError_t cluster_launch(void (*kernel)(Args...), int ncta, int nshots, size_t smem, cudaStream_t st,
+                           Args... args)
 {
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(kClusterCtas * nshots);
+    cfg.gridDim = dim3(ncta * nshots);
     cfg.blockDim = dim3(kClusterThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.x = ncta;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
@@ -272,14 +273,14 @@ bool cluster_shot_fits(int nx_max, int nz)
             cudaGetLastError();
             return false;
         }
-    // clusters of kClusterCtas CTAs with this much shared memory each must fit on the device
+    // clusters of p.ncta CTAs with this much shared memory each must fit on the device
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(kClusterCtas);
+    cfg.gridDim = dim3(p.ncta);
     cfg.blockDim = dim3(kClusterThreads);
     cfg.dynamicSmemBytes = p.smem_adj;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = kClusterCtas;
+    at[0].val.clusterDim.x = p.ncta;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
@@ -298,9 +299,9 @@ cudaError_t launch_cluster_forward(const Batch<float> &b, int nx_max, int ntb, b
     if (!cluster_plan(nx_max, b.nz, cluster_smem_limit(), p)) return cudaErrorInvalidValue;
     const int img = images ? 1 : 0;
     switch (b.store_type) {
-    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
-    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
-    default: return cluster_launch(k_cluster_fwd<kStoreNative>, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
+    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, p.ncta, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
+    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, p.ncta, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
+    default: return cluster_launch(k_cluster_fwd<kStoreNative>, p.ncta, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
     }
 }
 
@@ -309,9 +310,9 @@ cudaError_t launch_cluster_adjoint(const Batch<float> &b, int nx_max, int ntb, c
     ClusterPlan p;
     if (!cluster_plan(nx_max, b.nz, cluster_smem_limit(), p)) return cudaErrorInvalidValue;
     switch (b.store_type) {
-    case kStoreHalf: return cluster_launch(k_cluster_adj<kStoreHalf>, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
-    case kStoreBf16: return cluster_launch(k_cluster_adj<kStoreBf16>, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
-    default: return cluster_launch(k_cluster_adj<kStoreNative>, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
+    case kStoreHalf: return cluster_launch(k_cluster_adj<kStoreHalf>, p.ncta, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
+    case kStoreBf16: return cluster_launch(k_cluster_adj<kStoreBf16>, p.ncta, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
+    default: return cluster_launch(k_cluster_adj<kStoreNative>, p.ncta, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
     }
 }
 
