@@ -45,28 +45,33 @@ constexpr int kClusterMaxCtas = 16;
 constexpr int kClusterThreads = 1024;
 constexpr int kClHalo = 2 * kRad;  // halo rows of the copied fields
 
-// CTAs, rows per CTA and shared-memory row pitch of a window nx wide on an nz-row grid.
-// Shared arrays: "haloed" ones carry kClHalo rows above and below the own rows, "banded" ones
-// kRad rows (the recomputed CPML fields), the rest only the own rows; the CPML coefficients sit
-// in shared tables by column and by banded row.
+// CTAs, rows per CTA and shared-memory row pitch of a window nx wide on an nz-row grid, for
+// images of elem bytes.  Shared arrays: "haloed" ones carry kClHalo rows above and below the
+// own rows, "banded" ones kRad rows (the recomputed CPML fields), the rest only the own rows;
+// the CPML coefficients sit in shared tables by column and by banded row.  Each step's images
+// pass through a staging area of the own rows (rows of whole 16-byte chunks): the forward
+// writes one and copies it out at the start of the next step, the adjoint prefetches into one
+// or two (abuf; two when they fit).
 struct ClusterPlan {
-    int ncta = 0, h = 0, pitch = 0;
+    int ncta = 0, h = 0, pitch = 0, abuf = 0;
     size_t smem_fwd = 0, smem_adj = 0;
 };
 
-// forward: F0 F1 haloed; PSZ banded; P0 P1 PSX VP VF ZX ZZ MH MP MN own
-// adjoint: UZ0 UZ1 haloed; YZ banded; LP LF WP WF UX0 UX1 ZX ZZ YX GH GP GN own (the model
-// coefficients read through the read-only cache)
+// forward: F0 F1 haloed; PSZ banded; P0 P1 PSX VP VF ZX ZZ MH MP MN own; the receiver row
+// adjoint: UZ0 UZ1 haloed; YZ banded; LP LF WP WF UX0 UX1 ZX ZZ YX MH MP MN own
 constexpr int kClFwdHaloed = 2, kClFwdOwn = 10;
 constexpr int kClAdjHaloed = 2, kClAdjOwn = 12;
 
-inline size_t cluster_smem(int h, int pitch, int haloed, int own)
+// floats of the arrays and tables (rounded to 16 bytes), then the image staging
+__host__ __device__ inline size_t cluster_floats(int h, int pitch, int haloed, int own, int extra_rows)
 {
-    const size_t rows = (size_t)haloed * (h + 2 * kClHalo) + (h + 2 * kRad) + (size_t)own * h;
-    return sizeof(float) * (rows * pitch + 2 * (size_t)pitch + 2 * (size_t)(h + 2 * kRad)) + 64;
+    const size_t rows = (size_t)haloed * (h + 2 * kClHalo) + (h + 2 * kRad) + (size_t)own * h + extra_rows;
+    return (rows * pitch + 2 * (size_t)pitch + 2 * (size_t)(h + 2 * kRad) + 3) / 4 * 4;
 }
+// elements of a staged image row: whole 16-byte chunks covering nx
+__host__ __device__ inline int cluster_img_pitch(int nx, int elem) { return (nx * elem + 15) / 16 * 16 / elem; }
 
-inline bool cluster_plan(int nx, int nz, size_t smem_limit, ClusterPlan &p)
+inline bool cluster_plan(int nx, int nz, int elem, size_t smem_limit, ClusterPlan &p)
 {
     const int nzi = nz - 8;
     if (nzi < kClHalo || nx < 9) return false;
@@ -74,8 +79,11 @@ inline bool cluster_plan(int nx, int nz, size_t smem_limit, ClusterPlan &p)
     p.ncta = nzi / kClHalo < kClusterMaxCtas ? nzi / kClHalo : kClusterMaxCtas;
     p.h = (nzi + p.ncta - 1) / p.ncta;
     p.pitch = (nx + 3) / 4 * 4;
-    p.smem_fwd = cluster_smem(p.h, p.pitch, kClFwdHaloed, kClFwdOwn);
-    p.smem_adj = cluster_smem(p.h, p.pitch, kClAdjHaloed, kClAdjOwn);
+    const size_t stage = (size_t)2 * p.h * cluster_img_pitch(nx, elem) * elem;  // G and H of one step
+    p.smem_fwd = sizeof(float) * cluster_floats(p.h, p.pitch, kClFwdHaloed, kClFwdOwn, 1) + stage;
+    const size_t adj = sizeof(float) * cluster_floats(p.h, p.pitch, kClAdjHaloed, kClAdjOwn, 0);
+    p.abuf = adj + 2 * stage <= smem_limit ? 2 : 1;
+    p.smem_adj = adj + p.abuf * stage;
     return p.smem_adj <= smem_limit && p.smem_fwd <= smem_limit;
 }
 
@@ -180,17 +188,27 @@ __device__ __forceinline__ void cl_tables(const Batch<float> &b, const ClGeom &g
     }
 }
 
-// Max over the CTA into *slot (values >= 0).
-__device__ __forceinline__ void cl_block_max(float v, float *slot)
+// 16-byte copies global -> shared that complete asynchronously (cp.async, waited with
+// cp.async.wait_group: a hardware wait, no polling)
+__device__ __forceinline__ void cl_cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cl_cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cl_cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Max over the CTA of v >= 0, pushed by thread 0 into slot k of every CTA's table (no remote
+// read after the barrier: each CTA reduces its own copy).
+__device__ __forceinline__ void cl_push_max(cg::cluster_group &cl, const ClGeom &g, float v, float *table)
 {
     __shared__ float wm[kClusterThreads / 32];
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = v;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float m = 0.f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, wm[w]);
-        *slot = m;
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < (blockDim.x >> 5) ? wm[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((int)threadIdx.x < g.ncta) *cl.map_shared_rank(table + g.k, (int)threadIdx.x) = v;
     }
 }
 
@@ -206,8 +224,28 @@ struct ClBand {
     }
 };
 
+// Staged images of one step (own rows, G then H, rows of ip elements) <-> the image store:
+// the 16-byte chunks of the CTA, one per thread and pass.  to_store: generic stores; else
+// cp.async loads (the caller commits and waits).
+template <typename SI, bool to_store>
+__device__ __forceinline__ void cl_stage_copy(const Batch<float> &b, const ClGeom &g, int ip, SI *stage, SI *imgp)
+{
+    const int nch = ip * (int)sizeof(SI) / 16, per = g.nrows * nch, n = 2 * per;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int arr = e >= per, r = e - arr * per, lr = r / nch, c = r - lr * nch;
+        uint4 *sp = reinterpret_cast<uint4 *>(stage + ((long)arr * g.h + lr) * ip) + c;
+        uint4 *gp = reinterpret_cast<uint4 *>(imgp + arr * b.slot + (long)(g.iz0 + lr) * b.pitch) + c;
+        if (to_store)
+            *gp = *sp;
+        else
+            cl_cp_async16(sp, gp);
+    }
+}
+
 // Forward of shot blockIdx.x / ncta of the batch through all its steps (global steps ntb - nt
-// .. ntb - 1); every step's images (img != 0) to slot g of the image store.
+// .. ntb - 1); every step's images (img != 0) to slot g of the image store.  Global stores of a
+// step (images, receivers) are staged in shared memory and issued at the start of the next
+// step, so that they are complete long before the release of the next cluster barrier.
 template <int ST>
 __global__ void __launch_bounds__(kClusterThreads, 1)
 k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
@@ -215,7 +253,7 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
     using Cd = Codec<float, ST>;
     using SI = typename Cd::S;
     extern __shared__ __align__(16) float csm[];
-    __shared__ float s_max[2];
+    __shared__ float s_all[2][kClusterMaxCtas];
     cg::cluster_group cl = cg::this_cluster();
     const int ncta = (int)cl.num_blocks();
     const int s = blockIdx.x / ncta;
@@ -230,11 +268,15 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
     float *const P0 = base, *const P1 = base + op, *const PSX = base + 2 * op, *const VP = base + 3 * op,
                  *const VF = base + 4 * op, *const ZX = base + 5 * op, *const ZZ = base + 6 * op,
                  *const MH = base + 7 * op, *const MP = base + 8 * op, *const MN = base + 9 * op;
-    float *const AX = base + 10 * op, *const BX = AX + pitch, *const AZ = BX + pitch, *const BZ = AZ + h + 2 * kRad;
-    const size_t total = 2 * hp + bp + 10 * op;
-    for (size_t i = threadIdx.x; i < total; i += blockDim.x) csm[i] = 0.f;
-    cl_tables(b, G, AX, BX, AZ, BZ);
+    float *const RB = base + 10 * op;  // the receiver row (own rows holding it)
+    float *const AX = RB + pitch, *const BX = AX + pitch, *const AZ = BX + pitch, *const BZ = AZ + h + 2 * kRad;
+    const size_t nfl = cluster_floats(h, pitch, kClFwdHaloed, kClFwdOwn, 1);
+    const int ip = cluster_img_pitch(nx, (int)sizeof(SI));
+    SI *const IMG = reinterpret_cast<SI *>(csm + nfl);
+    const size_t stage_words = (size_t)2 * h * ip * sizeof(SI) / 4;
+    for (size_t i = threadIdx.x; i < nfl + stage_words; i += blockDim.x) csm[i] = 0.f;
     __syncthreads();
+    cl_tables(b, G, AX, BX, AZ, BZ);
     for (ClWalk w(G); w.on(); w.next()) {
         const long mi = (long)(G.iz0 + w.lr) * b.mpitch + sh.x0 + w.ix;
         const int i = w.lr * pitch + w.ix;
@@ -245,17 +287,29 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
     cl.sync();  // every CTA's state zeroed before any neighbour reads it
     const float inv_dh = b.inv_dh, inv_dh2 = b.inv_dh2;
     const int nrec = sh.rx1 - sh.rx0;
+    const bool has_rec = sh.rz >= G.iz0 && sh.rz < G.iz0 + G.nrows;
     const int zb = nz - cpml;  // first row of the bottom layer
     const ClBand band(G, zb);
     const int nbx = cpml > 4 ? min(2 * (cpml - 4), G.nxi) : 0;  // side-band columns of a row
+    SI *const imgb = img ? (SI *)b.store + (long)s * b.n_img * 2 * b.slot : nullptr;
     float amax = 0.f;  // max |P|, |F| after the previous step, over the shot
+    float wv_next = sh.nt > 0 ? b.wavelet[0] : 0.f;
     int cur = 0;
     for (int it = 0; it < sh.nt; it++) {
         const int g = it + ntb - sh.nt;
         // the current level and the next (selected, not indexed: no local-memory arrays)
         float *const Pc = cur ? P1 : P0, *const Fc = cur ? F1 : F0;
         float *const Pn = cur ? P0 : P1, *const Fn = cur ? F0 : F1;
+        const float wv = wv_next;
+        if (it + 1 < sh.nt) wv_next = b.wavelet[it + 1];
         cl_fill_halo(cl, G, Fc);
+        // the previous step's images and receiver values, staged, to global memory
+        if (it > 0) {
+            if (img) cl_stage_copy<SI, true>(b, G, ip, IMG, imgb + (long)(g - 1) * 2 * b.slot);
+            if (has_rec)
+                for (int t = threadIdx.x; t < nrec; t += blockDim.x)
+                    b.rec[sh.rec_off + (long)(it - 1) * nrec + t] = RB[sh.rx0 + t];
+        }
         __syncthreads();
         // psi (src/parallelcalls.cu:48-63): x of the side-band points of the own rows ...
         for (int q = threadIdx.x; q < G.nrows * nbx; q += blockDim.x) {
@@ -273,8 +327,6 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
         __syncthreads();
         const float sc = Cd::scaled ? image_scale(amax, inv_dh2) : 1.f;
         if (img && Cd::scaled && G.k == 0 && threadIdx.x == 0) b.scale[(long)s * b.nt_max + g] = sc;
-        const float wv = b.wavelet[it];
-        SI *imgp = img ? (SI *)b.store + ((long)s * b.n_img + g) * 2 * b.slot : nullptr;
         float lmax = 0.f;
         bool sat = false;
         for (ClWalk w(G); w.on(); w.next()) {
@@ -309,33 +361,41 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
             Pn[i] = nP;
             Fn[ih] = nF;
             if (Cd::scaled) lmax = fmaxf(lmax, fmaxf(fabsf(nP), fabsf(nF)));
-            if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1)
-                b.rec[sh.rec_off + (long)it * nrec + ix - sh.rx0] = nP + nF;
+            if (iz == sh.rz) RB[ix] = nP + nF;
             if (img) {
-                const long o = (long)iz * b.pitch + ix;
-                imgp[o] = Cd::enc_flag(Gv, sc, sat);
-                imgp[b.slot + o] = Cd::enc_flag(Hv, sc, sat);
+                IMG[w.lr * ip + ix] = Cd::enc_flag(Gv, sc, sat);
+                IMG[(h + w.lr) * ip + ix] = Cd::enc_flag(Hv, sc, sat);
             }
         }
         if (sat) atomicOr(b.status, kStatusSaturated);
-        if (Cd::scaled) cl_block_max(lmax, &s_max[it & 1]);
+        if (Cd::scaled) cl_push_max(cl, G, lmax, s_all[it & 1]);
         cl.sync();  // the new level, and every CTA's max, complete
         if (Cd::scaled) {
             float m = 0.f;
-            for (int r = 0; r < G.ncta; r++) m = fmaxf(m, *cl.map_shared_rank(&s_max[it & 1], r));
+            for (int r = 0; r < G.ncta; r++) m = fmaxf(m, s_all[it & 1][r]);
             amax = m;
             if (G.k == 0 && threadIdx.x == 0) b.amax[(long)s * (b.nt_max + 1) + g + 1] = m;
         }
         cur ^= 1;
     }
+    if (sh.nt > 0) {  // the last step's staged images and receiver values
+        if (img) cl_stage_copy<SI, true>(b, G, ip, IMG, imgb + (long)(ntb - 1) * 2 * b.slot);
+        if (has_rec)
+            for (int t = threadIdx.x; t < nrec; t += blockDim.x)
+                b.rec[sh.rec_off + (long)(sh.nt - 1) * nrec + t] = RB[sh.rx0 + t];
+    }
     cl.sync();  // no CTA leaves while a neighbour may still read its shared memory
 }
 
 // Exact adjoint of shot blockIdx.x / ncta with imaging from the image store (slot of each
-// global step), the residual in b.rec; the shot's gradient accumulated into its slot s of b.g
-// (zeroed by the caller).
+// global step), the residual in b.rec; the shot's gradient added into its slot s of b.g (zeroed
+// by the caller).  Each step's images are prefetched into shared memory with cp.async (one
+// step ahead when two staging buffers fit); the imaging of a step runs at the start of the
+// next one and adds into the gradient with fire-and-forget reductions, so that no global
+// memory operation is pending at a cluster barrier.
 template <int ST>
-__global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float> b, int ntb, int h, int pitch)
+__global__ void __launch_bounds__(kClusterThreads, 1)
+k_cluster_adj(Batch<float> b, int ntb, int h, int pitch, int abuf)
 {
     using Cd = Codec<float, ST>;
     using SI = typename Cd::S;
@@ -353,11 +413,32 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float>
     float *const base = YZ + bp;
     float *const LP = base, *const LF = base + op, *const WP = base + 2 * op, *const WF = base + 3 * op,
                  *const UX0 = base + 4 * op, *const UX1 = base + 5 * op, *const ZX = base + 6 * op,
-                 *const ZZ = base + 7 * op, *const YX = base + 8 * op;
-    float *const AX = base + 9 * op, *const BX = AX + pitch, *const AZ = BX + pitch, *const BZ = AZ + h + 2 * kRad;
-    const size_t total = 2 * hp + bp + 9 * op;
-    for (size_t i = threadIdx.x; i < total; i += blockDim.x) csm[i] = 0.f;
+                 *const ZZ = base + 7 * op, *const YX = base + 8 * op, *const MH = base + 9 * op,
+                 *const MP = base + 10 * op, *const MN = base + 11 * op;
+    float *const AX = base + 12 * op, *const BX = AX + pitch, *const AZ = BX + pitch, *const BZ = AZ + h + 2 * kRad;
+    const size_t nfl = cluster_floats(h, pitch, kClAdjHaloed, kClAdjOwn, 0);
+    const int ip = cluster_img_pitch(nx, (int)sizeof(SI));
+    const long stage = (long)2 * h * ip;  // elements of one staging buffer
+    SI *const IMG = reinterpret_cast<SI *>(csm + nfl);
+    for (size_t i = threadIdx.x; i < nfl; i += blockDim.x) csm[i] = 0.f;
+    __syncthreads();
     cl_tables(b, G, AX, BX, AZ, BZ);
+    for (ClWalk w(G); w.on(); w.next()) {
+        const long mi = (long)(G.iz0 + w.lr) * b.mpitch + sh.x0 + w.ix;
+        const int i = w.lr * pitch + w.ix;
+        MH[i] = b.mh[mi];
+        MP[i] = b.mp[mi];
+        MN[i] = b.mn[mi];
+    }
+    const SI *const imgb = (const SI *)b.store + (long)s * b.n_img * 2 * b.slot;
+    // the image of adjoint step j (global step ntb - 1 - j) into buffer j % abuf
+    auto prefetch = [&](int j) {
+        if (j < sh.nt)
+            cl_stage_copy<SI, false>(b, G, ip, IMG + (j % abuf) * stage,
+                                     const_cast<SI *>(imgb) + (long)(ntb - 1 - j) * 2 * b.slot);
+        cl_cp_commit();
+    };
+    if (abuf == 2) prefetch(0);
     cl.sync();
     const float inv_dh = b.inv_dh, inv_dh2 = b.inv_dh2, kk = b.img_scale;
     const int nrec = sh.rx1 - sh.rx0;
@@ -369,14 +450,31 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float>
     using C = Coef<float>;
     // band membership of a point (x side layers or the bottom layer)
     auto in_band = [&](int ix, int iz) { return ix < cpml || ix > nx - cpml - 1 || iz >= zb; };
+    // imaging of step j from its staged images and lambda of that step (in LP, LF)
+    auto imaging = [&](int j, float inv_sc) {
+        const SI *const Gs = IMG + (j % abuf) * stage, *const Hs = Gs + (long)h * ip;
+        for (ClWalk w(G); w.on(); w.next()) {
+            const int i = w.lr * pitch + w.ix, si = w.lr * ip + w.ix;
+            const long o = (long)(G.iz0 + w.lr) * b.pitch + w.ix;
+            const float lp = LP[i], lf = LF[i];
+            const float Gv = Cd::dec(Gs[si], inv_sc), Hv = Cd::dec(Hs[si], inv_sc);
+            atomicAdd(g0 + o, kk * Gv * lp);
+            atomicAdd(g1 + o, kk * Hv * (lp + lf));
+            atomicAdd(g2 + o, kk * Gv * lf);
+        }
+    };
+    float inv_sc_prev = 1.f;  // image scale of the previous step, inverted
     int cur = 0;  // u of this step in UX0 / UZ0 (cur 0) or UX1 / UZ1; zero before the first step
     for (int j = 0; j < sh.nt; j++) {
         const int m = sh.nt - j;
         const int g_img = ntb - 1 - j;  // global step of the image this iteration pairs with
+        const float inv_sc = Cd::scaled ? 1.f / b.scale[(long)s * b.nt_max + g_img] : 1.f;
         float *const UXc = cur ? UX1 : UX0, *const UZc = cur ? UZ1 : UZ0;
         float *const UXn = cur ? UX0 : UX1, *const UZn = cur ? UZ0 : UZ1;
         cl_fill_halo(cl, G, UZc);
-        __syncthreads();
+        if (j > 0) imaging(j - 1, inv_sc_prev);
+        __syncthreads();  // the buffer of step j - 1 free again
+        prefetch(j + abuf - 1);
         // Y of the band points: Y' = -D(w) + b Y with w = u at band points, 0 elsewhere; x of the
         // side-band points of the own rows ...
         for (int q = threadIdx.x; q < G.nrows * nbx; q += blockDim.x) {
@@ -403,20 +501,14 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float>
                               C::d1_3 * (wzv(3) - wzv(-3)) - C::d1_4 * (wzv(4) - wzv(-4));
             YZ[ib] = -(dwz * inv_dh) + BZ[r + kRad] * YZ[ib];
         }
+        if (abuf == 2) cl_cp_wait<1>();  // this step's images (the next step's may still fly)
+        else cl_cp_wait<0>();
         __syncthreads();
-        // lambda^m: increments += Dxx(u) - Dx(a Y) (and z), residual at the receivers; imaging;
-        // then g, h, Z and u of the next step from the new lambda
-        float inv_sc = 1.f;
-        if (Cd::scaled) inv_sc = 1.f / b.scale[(long)s * b.nt_max + g_img];
-        const SI *imgp = (const SI *)b.store + ((long)s * b.n_img + g_img) * 2 * b.slot;
+        // lambda^m: increments += Dxx(u) - Dx(a Y) (and z), residual at the receivers; then g, h,
+        // Z and u of the next step from the new lambda
         for (ClWalk w(G); w.on(); w.next()) {
             const int ix = w.ix, iz = G.iz0 + w.lr, i = w.lr * pitch + ix, ih = (w.lr + kClHalo) * pitch + ix;
             const int rb = w.lr + kRad, ib = rb * pitch + ix;
-            const long o = (long)iz * b.pitch + ix;
-            const long mi = (long)iz * b.mpitch + sh.x0 + ix;
-            const float Gv = Cd::dec(imgp[o], inv_sc), Hv = Cd::dec(imgp[b.slot + o], inv_sc);
-            const float mh = __ldg(b.mh + mi), mp = __ldg(b.mp + mi), mn = __ldg(b.mn + mi);
-            const float gh = g0[o], gp = g1[o], gn = g2[o];
             const float dxx = cl_d2(UXc + i, 1) * inv_dh2, dzz = cl_d2(UZc + ih, pitch) * inv_dh2;
             float wp, wf;
             if (ix < cpml + 4 || ix > nx - cpml - 5 || iz >= zb - 4) {  // a CPML coefficient within reach
@@ -442,11 +534,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float>
             const float lp = LP[i] + wp, lf = LF[i] + wf;
             LP[i] = lp;
             LF[i] = lf;
-            g0[o] = gh + kk * Gv * lp;
-            g1[o] = gp + kk * Hv * (lp + lf);
-            g2[o] = gn + kk * Gv * lf;
             // u of the next step: g = v_hor lP + v_nmo lF, h = v_po (lP + lF) (dt^2 folded in)
-            const float gx = mh * lp + mn * lf, hz = mp * (lp + lf);
+            const float gx = MH[i] * lp + MN[i] * lf, hz = MP[i] * (lp + lf);
             float ux = gx, uzv = hz;
             if (in_band(ix, iz)) {
                 const float zx = gx + BX[ix] * ZX[i];
@@ -460,8 +549,12 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_adj(Batch<float>
             UZn[ih] = uzv;
         }
         cl.sync();  // lambda and u of the next step complete in every CTA
+        inv_sc_prev = inv_sc;
         cur ^= 1;
     }
+    if (sh.nt > 0) imaging(sh.nt - 1, inv_sc_prev);
+    cl_cp_wait<0>();  // nothing in flight at exit (an empty group when the prefetch ran past the end)
+    cl.sync();  // no CTA leaves while a neighbour may still read its shared memory
 }
 
 }  // namespace fwi

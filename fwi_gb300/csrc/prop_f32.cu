@@ -257,18 +257,19 @@ size_t cluster_smem_limit()
     return (size_t)v - 1024;  // the kernels' static shared memory
 }
 
+int store_elem_bytes(int store_type) { return store_type == kStoreNative ? (int)sizeof(float) : 2; }
+
 }  // namespace
 
-bool cluster_shot_fits(int nx_max, int nz)
+bool cluster_shot_fits(int nx_max, int nz, int store_type)
 {
     ClusterPlan p;
-    if (!cluster_plan(nx_max, nz, cluster_smem_limit(), p)) return false;
-    for (cudaError_t e : {cluster_attrs(k_cluster_fwd<kStoreNative>, p.smem_fwd),
-                          cluster_attrs(k_cluster_fwd<kStoreHalf>, p.smem_fwd),
-                          cluster_attrs(k_cluster_fwd<kStoreBf16>, p.smem_fwd),
-                          cluster_attrs(k_cluster_adj<kStoreNative>, p.smem_adj),
-                          cluster_attrs(k_cluster_adj<kStoreHalf>, p.smem_adj),
-                          cluster_attrs(k_cluster_adj<kStoreBf16>, p.smem_adj)})
+    if (!cluster_plan(nx_max, nz, store_elem_bytes(store_type), cluster_smem_limit(), p)) return false;
+    // every kernel may take the device's whole opt-in shared memory: one setting serves all widths
+    const size_t lim = cluster_smem_limit();
+    for (cudaError_t e : {cluster_attrs(k_cluster_fwd<kStoreNative>, lim), cluster_attrs(k_cluster_fwd<kStoreHalf>, lim),
+                          cluster_attrs(k_cluster_fwd<kStoreBf16>, lim), cluster_attrs(k_cluster_adj<kStoreNative>, lim),
+                          cluster_attrs(k_cluster_adj<kStoreHalf>, lim), cluster_attrs(k_cluster_adj<kStoreBf16>, lim)})
         if (e != cudaSuccess) {
             cudaGetLastError();
             return false;
@@ -296,23 +297,28 @@ bool cluster_shot_fits(int nx_max, int nz)
 cudaError_t launch_cluster_forward(const Batch<float> &b, int nx_max, int ntb, bool images, cudaStream_t st)
 {
     ClusterPlan p;
-    if (!cluster_plan(nx_max, b.nz, cluster_smem_limit(), p)) return cudaErrorInvalidValue;
-    const int img = images ? 1 : 0;
+    if (!cluster_plan(nx_max, b.nz, store_elem_bytes(b.store_type), cluster_smem_limit(), p))
+        return cudaErrorInvalidValue;
+    const int img = images ? 1 : 0, n = p.ncta;
+    const size_t sm = p.smem_fwd;
     switch (b.store_type) {
-    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, p.ncta, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
-    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, p.ncta, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
-    default: return cluster_launch(k_cluster_fwd<kStoreNative>, p.ncta, b.B, p.smem_fwd, st, b, ntb, p.h, p.pitch, img);
+    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, n, b.B, sm, st, b, ntb, p.h, p.pitch, img);
+    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, n, b.B, sm, st, b, ntb, p.h, p.pitch, img);
+    default: return cluster_launch(k_cluster_fwd<kStoreNative>, n, b.B, sm, st, b, ntb, p.h, p.pitch, img);
     }
 }
 
 cudaError_t launch_cluster_adjoint(const Batch<float> &b, int nx_max, int ntb, cudaStream_t st)
 {
     ClusterPlan p;
-    if (!cluster_plan(nx_max, b.nz, cluster_smem_limit(), p)) return cudaErrorInvalidValue;
+    if (!cluster_plan(nx_max, b.nz, store_elem_bytes(b.store_type), cluster_smem_limit(), p))
+        return cudaErrorInvalidValue;
+    const int n = p.ncta, ab = p.abuf;
+    const size_t sm = p.smem_adj;
     switch (b.store_type) {
-    case kStoreHalf: return cluster_launch(k_cluster_adj<kStoreHalf>, p.ncta, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
-    case kStoreBf16: return cluster_launch(k_cluster_adj<kStoreBf16>, p.ncta, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
-    default: return cluster_launch(k_cluster_adj<kStoreNative>, p.ncta, b.B, p.smem_adj, st, b, ntb, p.h, p.pitch);
+    case kStoreHalf: return cluster_launch(k_cluster_adj<kStoreHalf>, n, b.B, sm, st, b, ntb, p.h, p.pitch, ab);
+    case kStoreBf16: return cluster_launch(k_cluster_adj<kStoreBf16>, n, b.B, sm, st, b, ntb, p.h, p.pitch, ab);
+    default: return cluster_launch(k_cluster_adj<kStoreNative>, n, b.B, sm, st, b, ntb, p.h, p.pitch, ab);
     }
 }
 
