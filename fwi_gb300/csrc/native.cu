@@ -1137,7 +1137,7 @@ template <typename T> struct Ctx : CtxBase {
             if (atoi(e) == 0) return false;
         for (const auto &c : cluster_fit)
             if (c.first == nxm) return c.second;
-        const bool ok = fwi::cluster_shot_fits(nxm, nz, store_type());
+        const bool ok = fwi::cluster_shot_fits(nxm, nz, cfg.cpml, store_type());
         cluster_fit.emplace_back(nxm, ok);
         return ok;
     }

@@ -217,7 +217,7 @@ cudaError_t prepare_fp32_kernels();
 // window nx wide on an nz-row grid fits the cluster's shared memory and
 // clusters of that size can run on the current device (FP32, exact adjoint,
 // full image storage).  The launches cover every shot of the batch view.
-bool cluster_shot_fits(int nx_max, int nz, int store_type);
+bool cluster_shot_fits(int nx_max, int nz, int cpml, int store_type);
 cudaError_t launch_cluster_forward(const Batch<float> &b, int nx_max, int ntb, bool images, cudaStream_t st);
 cudaError_t launch_cluster_adjoint(const Batch<float> &b, int nx_max, int ntb, cudaStream_t st);
 

@@ -6,34 +6,44 @@
 // is a few microseconds of work, less than the launch and dependency latency
 // of the two tile passes.  Here a cluster of up to 16 CTAs (a non-portable
 // cluster size, enabled per kernel) takes one shot through all its time steps
-// in a single launch.  CTA k owns the interior rows [4 + k h, 4 + (k + 1) h)
-// of the shot's window (h >= 8), every column, and keeps the state of its rows
-// in its own shared memory.  After each step's cluster barrier (barrier.cluster:
-// hardware, release / acquire over the cluster's shared memory) it copies the
-// 8 rows above and below its own of the one field the next step's z-stencils
-// need from the neighbours' shared memory (distributed shared memory) and
-// recomputes the CPML auxiliary field of the 4 rows either side itself, so
-// that a step needs a single cluster barrier.  No other wait exists, and
-// every thread of every CTA runs the same number of steps and barriers.
+// in a single launch.  CTA k owns a band of interior rows of the shot's window
+// (at least 8; the partition balances a cost model of the CPML work, so the
+// CTAs at the bottom layer hold fewer rows), every column, and keeps the state
+// of its rows in its own shared memory.  The one field the next step's
+// z-stencils need from other CTAs is written, for the 8 rows next to each
+// edge, straight into the neighbours' halo rows as it is computed (stores to
+// distributed shared memory), and each CTA recomputes the CPML auxiliary field
+// of the 4 rows either side of its own itself, so that a step needs a single
+// cluster barrier (barrier.cluster: hardware, release / acquire over the
+// cluster's shared memory) and no copy.  No other wait exists, and every
+// thread of every CTA runs the same number of steps and barriers.
 //
-// Forward step: copy the 8-row halo of F; psi_x of the band points of the own
-// rows, psi_z of the band points of the own rows and 4 either side; zeta, the
-// increment update, the next level into the other half of a ping-pong pair,
-// receivers, images and the CTA's max of |P|, |F|; barrier; every CTA reads
-// all CTAs' maxima (the next step's image scale).  Exact adjoint step: copy
-// the 8-row halo of u_z; Y_x of the own band points, Y_z of the band points of
-// the own rows and 4 either side; the increment and lambda update, residual
-// injection, imaging, and then at once the next step's g, h, Z and fields u
-// from the new lambda (into the other half of a ping-pong pair); barrier.
-// Both fields the halos come from are double-buffered, so a neighbour's copy
-// of step t and the owner's writes of step t + 1 never meet.  The arithmetic
-// is the tile passes' (difference-form Laplacian, increment-form leapfrog, the
-// same CPML recursions), evaluated in another order: results agree with them
-// to FP32 rounding; the recomputed halo values are bit-identical to the
-// owner's (same inputs, same operations).
+// Forward step: the previous step's staged images and receiver values out to
+// global memory; psi_x of the band points of the own rows, psi_z of the band
+// points of the own rows and 4 either side; zeta, the increment update, the
+// next level into the other half of a ping-pong pair (and the neighbours'
+// halos), receivers and images into shared staging, the CTA's max of |P|,
+// |F| pushed to every CTA; barrier; the next step's image scale from the
+// maxima.  Exact adjoint step: the next step's images prefetched (cp.async);
+// Y_x of the own band points, Y_z of the band points of the own rows and 4
+// either side; the increment and lambda update, residual injection, imaging
+// (reductions into the gradient, fire-and-forget), and then at once the next
+// step's g, h, Z and fields u from the new lambda (into the other half of a
+// ping-pong pair, and the neighbours' halos); barrier.  Both fields with halos
+// are double-buffered, so that a neighbour's write of step t + 1 never meets
+// the owner's reads of step t.  Global stores and reductions are issued early
+// in a step or spread over it, not at its end, so that the barrier's release
+// seldom waits for them.  The arithmetic is the tile passes' (difference-form
+// Laplacian, increment-form leapfrog, the same CPML recursions), evaluated in
+// another order: results agree with them to FP32 rounding; the recomputed
+// CPML rows are bit-identical to the owner's (same inputs, same operations).
 #pragma once
 
 #include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
 
 #include "prop_tma.cuh"
 
@@ -42,19 +52,26 @@ namespace fwi {
 namespace cg = cooperative_groups;
 
 constexpr int kClusterMaxCtas = 16;
-constexpr int kClusterThreads = 1024;
+constexpr int kClusterThreads = 704;  // 4 columns a thread: one pass over a CTA of C1's rows
 constexpr int kClHalo = 2 * kRad;  // halo rows of the copied fields
 
-// CTAs, rows per CTA and shared-memory row pitch of a window nx wide on an nz-row grid, for
-// images of elem bytes.  Shared arrays: "haloed" ones carry kClHalo rows above and below the
-// own rows, "banded" ones kRad rows (the recomputed CPML fields), the rest only the own rows;
-// the CPML coefficients sit in shared tables by column and by banded row.  Each step's images
-// pass through a staging area of the own rows (rows of whole 16-byte chunks): the forward
-// writes one and copies it out at the start of the next step, the adjoint prefetches into one
-// or two (abuf; two when they fit).
+// Interior rows of each CTA: CTA k owns interior rows [start[k], start[k + 1]) (global rows
+// 4 + start[k] ...), at least kClHalo of them when the cluster has more than one CTA.
+struct ClRows {
+    int start[kClusterMaxCtas + 1];
+};
+
+// CTAs, their rows, the largest CTA's row count h and the shared-memory row pitch of a window nx
+// wide on an nz-row grid with a cpml-wide layer, for images of elem bytes.  Shared arrays:
+// "haloed" ones carry kClHalo rows above and below the own rows, "banded" ones kRad rows (the
+// recomputed CPML fields), the rest only the own rows; the CPML coefficients sit in shared
+// tables by column and by banded row.  Each step's images pass through a staging area of the
+// own rows (rows of whole 16-byte chunks): the forward writes one and copies it out at the start
+// of the next step, the adjoint prefetches into one or two (abuf; two when they fit).
 struct ClusterPlan {
     int ncta = 0, h = 0, pitch = 0, abuf = 0;
     size_t smem_fwd = 0, smem_adj = 0;
+    ClRows rows{};
 };
 
 // forward: F0 F1 haloed; PSZ banded; P0 P1 PSX VP VF ZX ZZ MH MP MN own; the receiver row
@@ -71,28 +88,107 @@ __host__ __device__ inline size_t cluster_floats(int h, int pitch, int haloed, i
 // elements of a staged image row: whole 16-byte chunks covering nx
 __host__ __device__ inline int cluster_img_pitch(int nx, int elem) { return (nx * elem + 15) / 16 * 16 / elem; }
 
-inline bool cluster_plan(int nx, int nz, int elem, size_t smem_limit, ClusterPlan &p)
+// Relative cost of one step of the CTA holding interior rows [a, a + n): passes of the main
+// phase over groups of 4 columns (a row within 4 of the bottom layer costs half as much again:
+// the CPML terms), plus the passes of the recomputed z-band rows and of the side-band columns.  A
+// model of the measured phase times, used only to balance the partition.
+inline double cluster_row_cost(int a, int n, int nx, int nz, int cpml)
+{
+    const double T = kClusterThreads;
+    const int nxi = nx - 8, nq = (nxi + 3) / 4, zb = nz - cpml, g0 = 4 + a, g1 = 4 + a + n;
+    const int heavy = std::max(0, g1 - std::max(g0, zb - 4));
+    // passes (the slowest warp) and work (issue slots) weigh half each
+    const double w = n * (double)nq / T, f = 1.0 + 0.5 * heavy / n;
+    double c = 0.5 * std::ceil(w) * f + 0.5 * w * f;
+    const int lo = std::max(std::max(4, zb), g0 - kRad), hi = std::min(nz - 4, g1 + kRad);
+    if (hi > lo) c += 0.5 * std::ceil((hi - lo) * (double)nq / T);
+    const int nbx = cpml > 4 ? std::min(2 * (cpml - 4), nxi) : 0;
+    if (nbx > 0) c += 0.3 * std::ceil(n * (double)nbx / T);
+    return c;
+}
+
+// Partition of nzi interior rows into ncta chunks of [lo, hcap] rows minimising the largest
+// chunk cost (dynamic programme over chunk ends).  Returns that cost, or a negative value if
+// no partition exists.
+inline double cluster_partition(int nzi, int ncta, int lo, int hcap, int nx, int nz, int cpml, ClRows &out)
+{
+    const double inf = 1e300;
+    std::vector<double> best((size_t)(ncta + 1) * (nzi + 1), inf);
+    std::vector<int> from((size_t)(ncta + 1) * (nzi + 1), -1);
+    best[0] = 0.0;
+    for (int k = 1; k <= ncta; k++)
+        for (int r = 1; r <= nzi; r++)
+            for (int n = lo; n <= std::min(hcap, r); n++) {
+                const double prev = best[(size_t)(k - 1) * (nzi + 1) + r - n];
+                if (prev >= inf) continue;
+                const double c = std::max(prev, cluster_row_cost(r - n, n, nx, nz, cpml));
+                double &cur = best[(size_t)k * (nzi + 1) + r];
+                if (c < cur - 1e-9) {
+                    cur = c;
+                    from[(size_t)k * (nzi + 1) + r] = r - n;
+                }
+            }
+    const double c = best[(size_t)ncta * (nzi + 1) + nzi];
+    if (c >= inf) return -1.0;
+    int r = nzi;
+    for (int k = ncta; k >= 1; k--) {
+        out.start[k] = r;
+        r = from[(size_t)k * (nzi + 1) + r];
+    }
+    out.start[0] = 0;
+    for (int k = ncta + 1; k <= kClusterMaxCtas; k++) out.start[k] = nzi;
+    return c;
+}
+
+inline bool cluster_plan(int nx, int nz, int cpml, int elem, size_t smem_limit, ClusterPlan &p)
 {
     const int nzi = nz - 8;
     if (nzi < kClHalo || nx < 9) return false;
-    // a halo comes from one neighbour only: h >= 8
-    p.ncta = nzi / kClHalo < kClusterMaxCtas ? nzi / kClHalo : kClusterMaxCtas;
-    p.h = (nzi + p.ncta - 1) / p.ncta;
+    // a halo comes from one neighbour only: every CTA holds at least 8 rows
+    p.ncta = std::min(kClusterMaxCtas, nzi / kClHalo);
     p.pitch = (nx + 3) / 4 * 4;
-    const size_t stage = (size_t)2 * p.h * cluster_img_pitch(nx, elem) * elem;  // G and H of one step
-    p.smem_fwd = sizeof(float) * cluster_floats(p.h, p.pitch, kClFwdHaloed, kClFwdOwn, 1) + stage;
-    const size_t adj = sizeof(float) * cluster_floats(p.h, p.pitch, kClAdjHaloed, kClAdjOwn, 0);
-    p.abuf = adj + 2 * stage <= smem_limit ? 2 : 1;
-    p.smem_adj = adj + p.abuf * stage;
+    const int ip = cluster_img_pitch(nx, elem);
+    auto fwd_bytes = [&](int h) {
+        return sizeof(float) * cluster_floats(h, p.pitch, kClFwdHaloed, kClFwdOwn, 1) + (size_t)2 * h * ip * elem;
+    };
+    auto adj_bytes = [&](int h, int abuf) {
+        return sizeof(float) * cluster_floats(h, p.pitch, kClAdjHaloed, kClAdjOwn, 0) +
+               (size_t)abuf * 2 * h * ip * elem;
+    };
+    int hmax = 0;
+    for (int h = kClHalo; h <= nzi && fwd_bytes(h) <= smem_limit && adj_bytes(h, 1) <= smem_limit; h++) hmax = h;
+    if (hmax == 0 || (long)hmax * p.ncta < nzi) return false;
+    // rows per CTA that leave room for two adjoint image buffers (the prefetch one step ahead),
+    // if such a partition exists
+    int hmax2 = 0;
+    for (int h = kClHalo; h <= hmax && adj_bytes(h, 2) <= smem_limit; h++) hmax2 = h;
+    if ((long)hmax2 * p.ncta >= nzi) hmax = hmax2;
+    const int lo = p.ncta > 1 ? kClHalo : nzi;
+    // the least cost, then the fewest rows per CTA (shared memory) that still reach it
+    const double cbest = cluster_partition(nzi, p.ncta, lo, hmax, nx, nz, cpml, p.rows);
+    if (cbest < 0) return false;
+    for (int hc = (nzi + p.ncta - 1) / p.ncta; hc < hmax; hc++) {
+        ClRows r{};
+        const double c = cluster_partition(nzi, p.ncta, lo, hc, nx, nz, cpml, r);
+        if (c >= 0 && c <= cbest + 1e-9) {
+            p.rows = r;
+            break;
+        }
+    }
+    p.h = 0;
+    for (int k = 0; k < p.ncta; k++) p.h = std::max(p.h, p.rows.start[k + 1] - p.rows.start[k]);
+    p.smem_fwd = fwd_bytes(p.h);
+    p.abuf = adj_bytes(p.h, 2) <= smem_limit ? 2 : 1;
+    p.smem_adj = adj_bytes(p.h, p.abuf);
     return p.smem_adj <= smem_limit && p.smem_fwd <= smem_limit;
 }
 
-// Geometry of one CTA's rows and the thread's walk over its points: point q = threadIdx.x +
-// n blockDim.x of the own rows x interior columns, stepped by carries instead of divisions.
+// Geometry of one CTA and its walk: point q = threadIdx.x + n blockDim.x of the own rows x
+// interior columns, stepped by carries instead of divisions.
 struct ClGeom {
-    int k, ncta, h, pitch, nx, nz, iz0, nrows, nxi, npts;
+    int k, ncta, h, pitch, nx, nz, iz0, nrows, nup, nxi, npts;
     int dlr, dix;  // blockDim.x = dlr rows + dix columns
-    __device__ void init(int k_, int ncta_, int h_, int pitch_, int nx_, int nz_)
+    __device__ void init(int k_, int ncta_, int h_, int pitch_, int nx_, int nz_, const ClRows &rows)
     {
         k = k_;
         ncta = ncta_;
@@ -100,8 +196,9 @@ struct ClGeom {
         pitch = pitch_;
         nx = nx_;
         nz = nz_;
-        iz0 = 4 + k * h;
-        nrows = max(0, min(h, nz - 4 - iz0));
+        iz0 = 4 + rows.start[k];
+        nrows = rows.start[k + 1] - rows.start[k];
+        nup = k > 0 ? rows.start[k] - rows.start[k - 1] : 0;
         nxi = nx - 8;
         npts = nrows * nxi;
         dlr = (int)blockDim.x / nxi;
@@ -132,41 +229,122 @@ struct ClWalk {
     }
 };
 
-// The kClHalo rows above and below the CTA's own of a haloed array (own row r at row
-// r + kClHalo) from the neighbours' own rows after a cluster barrier; frame rows read zero.
-__device__ __forceinline__ void cl_fill_halo(cg::cluster_group &cl, const ClGeom &g, float *a)
-{
-    const int p4 = g.pitch / 4, n = 2 * kClHalo * p4;
-    const float4 *up = g.k > 0 ? reinterpret_cast<const float4 *>(cl.map_shared_rank(a, g.k - 1)) : nullptr;
-    const float4 *down = g.k + 1 < g.ncta ? reinterpret_cast<const float4 *>(cl.map_shared_rank(a, g.k + 1)) : nullptr;
-    float4 *a4 = reinterpret_cast<float4 *>(a);
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int hr = e / p4, c = e - hr * p4;
-        if (hr < kClHalo) {  // global row iz0 - 8 + hr: the upper neighbour's own row h - 8 + hr
-            const int iz = g.iz0 - kClHalo + hr;
-            a4[hr * p4 + c] = (iz >= 4 && up) ? up[(g.h + hr) * p4 + c] : z;
-        } else {  // global row iz0 + h + hr - 8: the lower neighbour's own row hr - 8
-            const int iz = g.iz0 + g.h + hr - kClHalo;
-            a4[(g.h + hr) * p4 + c] = (iz < g.nz - 4 && down) ? down[hr * p4 + c] : z;
-        }
-    }
-}
-
-// 8th-order derivatives (unnormalised) at c along stride st (1: x, the pitch: z).  Difference
-// form for the second derivative, as the tile passes.
-__device__ __forceinline__ float cl_d2(const float *c, int st)
+// 8th-order derivatives (unnormalised) from the centre o and the values k = 1..4 points after
+// (pk) and before (mk).  Difference form for the second derivative, as the tile passes.  Every
+// stencil of this file goes through these two, so that the scalar and the 4-column forms give
+// the same results.
+__device__ __forceinline__ float cl_d2v(float o, float p1, float m1, float p2, float m2, float p3, float m3, float p4,
+                                        float m4)
 {
     using C = Coef<float>;
-    const float o = c[0];
-    return C::d2_1 * ((c[st] - o) + (c[-st] - o)) - C::d2_2 * ((c[2 * st] - o) + (c[-2 * st] - o)) +
-           C::d2_3 * ((c[3 * st] - o) + (c[-3 * st] - o)) - C::d2_4 * ((c[4 * st] - o) + (c[-4 * st] - o));
+    return C::d2_1 * ((p1 - o) + (m1 - o)) - C::d2_2 * ((p2 - o) + (m2 - o)) + C::d2_3 * ((p3 - o) + (m3 - o)) -
+           C::d2_4 * ((p4 - o) + (m4 - o));
+}
+__device__ __forceinline__ float cl_d1v(float p1, float m1, float p2, float m2, float p3, float m3, float p4, float m4)
+{
+    using C = Coef<float>;
+    return C::d1_1 * (p1 - m1) - C::d1_2 * (p2 - m2) + C::d1_3 * (p3 - m3) - C::d1_4 * (p4 - m4);
+}
+// the same at c along stride st (1: x, the pitch: z)
+__device__ __forceinline__ float cl_d2(const float *c, int st)
+{
+    return cl_d2v(c[0], c[st], c[-st], c[2 * st], c[-2 * st], c[3 * st], c[-3 * st], c[4 * st], c[-4 * st]);
 }
 __device__ __forceinline__ float cl_d1(const float *c, int st)
 {
-    using C = Coef<float>;
-    return C::d1_1 * (c[st] - c[-st]) - C::d1_2 * (c[2 * st] - c[-2 * st]) + C::d1_3 * (c[3 * st] - c[-3 * st]) -
-           C::d1_4 * (c[4 * st] - c[-4 * st]);
+    return cl_d1v(c[st], c[-st], c[2 * st], c[-2 * st], c[3 * st], c[-3 * st], c[4 * st], c[-4 * st]);
+}
+
+// Four consecutive floats (16-byte aligned) to and from registers.
+__device__ __forceinline__ void cl_ld4(float (&v)[4], const float *p)
+{
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+}
+__device__ __forceinline__ void cl_st4(float *p, const float (&v)[4])
+{
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+// x window of 12 values around the 4 columns at p (p[-4] .. p[7])
+__device__ __forceinline__ void cl_ld12(float (&w)[12], const float *p)
+{
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float4 t = *reinterpret_cast<const float4 *>(p - 4 + 4 * c);
+        w[4 * c] = t.x;
+        w[4 * c + 1] = t.y;
+        w[4 * c + 2] = t.z;
+        w[4 * c + 3] = t.w;
+    }
+}
+// derivatives of column j (0..3) of a window (centre w[4 + j])
+__device__ __forceinline__ float cl_d2w(const float (&w)[12], int j)
+{
+    return cl_d2v(w[4 + j], w[5 + j], w[3 + j], w[6 + j], w[2 + j], w[7 + j], w[1 + j], w[8 + j], w[j]);
+}
+__device__ __forceinline__ float cl_d1w(const float (&w)[12], int j)
+{
+    return cl_d1v(w[5 + j], w[3 + j], w[6 + j], w[2 + j], w[7 + j], w[1 + j], w[8 + j], w[j]);
+}
+// z derivatives of 4 columns at p (stride the pitch), into d[0..3]
+__device__ __forceinline__ void cl_d2z4(float (&d)[4], const float *p, int st)
+{
+    float o[4], a[4], b2[4], c[4], e[4], f[4], g[4], h[4], k[4];
+    cl_ld4(o, p);
+    cl_ld4(a, p + st);
+    cl_ld4(b2, p - st);
+    cl_ld4(c, p + 2 * st);
+    cl_ld4(e, p - 2 * st);
+    cl_ld4(f, p + 3 * st);
+    cl_ld4(g, p - 3 * st);
+    cl_ld4(h, p + 4 * st);
+    cl_ld4(k, p - 4 * st);
+#pragma unroll
+    for (int j = 0; j < 4; j++) d[j] = cl_d2v(o[j], a[j], b2[j], c[j], e[j], f[j], g[j], h[j], k[j]);
+}
+__device__ __forceinline__ void cl_d1z4(float (&d)[4], const float *p, int st)
+{
+    float a[4], b2[4], c[4], e[4], f[4], g[4], h[4], k[4];
+    cl_ld4(a, p + st);
+    cl_ld4(b2, p - st);
+    cl_ld4(c, p + 2 * st);
+    cl_ld4(e, p - 2 * st);
+    cl_ld4(f, p + 3 * st);
+    cl_ld4(g, p - 3 * st);
+    cl_ld4(h, p + 4 * st);
+    cl_ld4(k, p - 4 * st);
+#pragma unroll
+    for (int j = 0; j < 4; j++) d[j] = cl_d1v(a[j], b2[j], c[j], e[j], f[j], g[j], h[j], k[j]);
+}
+
+// Four image values to a 16-byte-or-8-byte aligned staging slot.
+__device__ __forceinline__ void cl_st4_img(float *p, float a, float b, float c, float d)
+{
+    *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+template <typename S> __device__ __forceinline__ void cl_st4_img(S *p, S a, S b, S c, S d)
+{
+    static_assert(sizeof(S) == 2, "2-byte image type");
+    unsigned short u[4];
+    memcpy(&u[0], &a, 2);
+    memcpy(&u[1], &b, 2);
+    memcpy(&u[2], &c, 2);
+    memcpy(&u[3], &d, 2);
+    *reinterpret_cast<uint2 *>(p) = make_uint2(u[0] | ((uint32_t)u[1] << 16), u[2] | ((uint32_t)u[3] << 16));
+}
+// Four image values from a staging slot.
+__device__ __forceinline__ void cl_ld4_img(float (&v)[4], const float *p) { cl_ld4(v, p); }
+template <typename S> __device__ __forceinline__ void cl_ld4_img(S (&v)[4], const S *p)
+{
+    static_assert(sizeof(S) == 2, "2-byte image type");
+    const uint2 t = *reinterpret_cast<const uint2 *>(p);
+    const unsigned short u[4] = {(unsigned short)(t.x & 0xffffu), (unsigned short)(t.x >> 16),
+                                 (unsigned short)(t.y & 0xffffu), (unsigned short)(t.y >> 16)};
+#pragma unroll
+    for (int j = 0; j < 4; j++) memcpy(&v[j], &u[j], 2);
 }
 
 // CPML coefficient tables of the CTA: by column (0 outside the side layers) and by banded row
@@ -215,12 +393,13 @@ __device__ __forceinline__ void cl_push_max(cg::cluster_group &cl, const ClGeom 
 // The banded rows of the CTA in z-band (bottom layer) that lie inside the interior: rows
 // r in [-4, h + 4) with global row iz0 + r in [max(4, zb), nz - 4); walked as r0 + q / nxi.
 struct ClBand {
-    int r0, npts;
+    int r0, nrows, npts;
     __device__ ClBand(const ClGeom &g, int zb)
     {
-        const int lo = max(max(4, zb), g.iz0 - kRad), hi = min(g.nz - 4, g.iz0 + g.h + kRad);
+        const int lo = max(max(4, zb), g.iz0 - kRad), hi = min(g.nz - 4, g.iz0 + g.nrows + kRad);
         r0 = lo - g.iz0;
-        npts = hi > lo ? (hi - lo) * g.nxi : 0;
+        nrows = hi > lo ? hi - lo : 0;
+        npts = nrows * g.nxi;
     }
 };
 
@@ -248,7 +427,7 @@ __device__ __forceinline__ void cl_stage_copy(const Batch<float> &b, const ClGeo
 // step, so that they are complete long before the release of the next cluster barrier.
 template <int ST>
 __global__ void __launch_bounds__(kClusterThreads, 1)
-k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
+k_cluster_fwd(Batch<float> b, const __grid_constant__ ClRows rows, int ntb, int h, int pitch, int img)
 {
     using Cd = Codec<float, ST>;
     using SI = typename Cd::S;
@@ -259,7 +438,7 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
     const int s = blockIdx.x / ncta;
     const DevShot sh = b.shots[s];
     ClGeom G;
-    G.init((int)cl.block_rank(), ncta, h, pitch, sh.nx, b.nz);
+    G.init((int)cl.block_rank(), ncta, h, pitch, sh.nx, b.nz, rows);
     const int nx = sh.nx, nz = b.nz, cpml = b.cpml;
     const size_t hp = (size_t)(h + 2 * kClHalo) * pitch, bp = (size_t)(h + 2 * kRad) * pitch,
                  op = (size_t)h * pitch;
@@ -291,6 +470,7 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
     const int zb = nz - cpml;  // first row of the bottom layer
     const ClBand band(G, zb);
     const int nbx = cpml > 4 ? min(2 * (cpml - 4), G.nxi) : 0;  // side-band columns of a row
+    const int nq = (G.nxi + 3) / 4;                               // groups of 4 columns of a row
     SI *const imgb = img ? (SI *)b.store + (long)s * b.n_img * 2 * b.slot : nullptr;
     float amax = 0.f;  // max |P|, |F| after the previous step, over the shot
     float wv_next = sh.nt > 0 ? b.wavelet[0] : 0.f;
@@ -300,17 +480,19 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
         // the current level and the next (selected, not indexed: no local-memory arrays)
         float *const Pc = cur ? P1 : P0, *const Fc = cur ? F1 : F0;
         float *const Pn = cur ? P0 : P1, *const Fn = cur ? F0 : F1;
+        // the neighbours' copies of the next level's rows next to this CTA's (their halo rows)
+        float *const Fn_up = G.k > 0 ? cl.map_shared_rank(Fn, G.k - 1) : nullptr;
+        float *const Fn_dn = G.k + 1 < G.ncta ? cl.map_shared_rank(Fn, G.k + 1) : nullptr;
         const float wv = wv_next;
         if (it + 1 < sh.nt) wv_next = b.wavelet[it + 1];
-        cl_fill_halo(cl, G, Fc);
-        // the previous step's images and receiver values, staged, to global memory
+        // the previous step's images and receiver values, staged, to global memory (the staging
+        // area is rewritten only after the barrier that ends phase A)
         if (it > 0) {
             if (img) cl_stage_copy<SI, true>(b, G, ip, IMG, imgb + (long)(g - 1) * 2 * b.slot);
             if (has_rec)
                 for (int t = threadIdx.x; t < nrec; t += blockDim.x)
                     b.rec[sh.rec_off + (long)(it - 1) * nrec + t] = RB[sh.rx0 + t];
         }
-        __syncthreads();
         // psi (src/parallelcalls.cu:48-63): x of the side-band points of the own rows ...
         for (int q = threadIdx.x; q < G.nrows * nbx; q += blockDim.x) {
             const int lr = q / nbx, c = q - lr * nbx;
@@ -318,53 +500,119 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
             const int i = lr * pitch + ix;
             PSX[i] = BX[ix] * PSX[i] + AX[ix] * (cl_d1(Pc + i, 1) * inv_dh);
         }
-        // ... z of the bottom-band points of the own rows and 4 either side
-        for (int q = threadIdx.x; q < band.npts; q += blockDim.x) {
-            const int rr = q / G.nxi, r = band.r0 + rr, ix = 4 + q - rr * G.nxi;
+        // ... z of the bottom-band points of the own rows and 4 either side, 4 columns a thread
+        for (int q = threadIdx.x; q < band.nrows * nq; q += blockDim.x) {
+            const int rr = q / nq, r = band.r0 + rr, ix = 4 + 4 * (q - rr * nq);
             const int ib = (r + kRad) * pitch + ix, ih = (r + kClHalo) * pitch + ix;
-            PSZ[ib] = BZ[r + kRad] * PSZ[ib] + AZ[r + kRad] * (cl_d1(Fc + ih, pitch) * inv_dh);
+            const int nval = min(4, nx - 4 - ix);  // columns inside the interior
+            float d[4], ps[4];
+            cl_d1z4(d, Fc + ih, pitch);
+            cl_ld4(ps, PSZ + ib);
+            const float bz = BZ[r + kRad], az = AZ[r + kRad];
+#pragma unroll
+            for (int j = 0; j < 4; j++) ps[j] = j < nval ? bz * ps[j] + az * (d[j] * inv_dh) : 0.f;
+            cl_st4(PSZ + ib, ps);
         }
         __syncthreads();
         const float sc = Cd::scaled ? image_scale(amax, inv_dh2) : 1.f;
         if (img && Cd::scaled && G.k == 0 && threadIdx.x == 0) b.scale[(long)s * b.nt_max + g] = sc;
         float lmax = 0.f;
         bool sat = false;
-        for (ClWalk w(G); w.on(); w.next()) {
-            const int ix = w.ix, iz = G.iz0 + w.lr, i = w.lr * pitch + ix, ih = (w.lr + kClHalo) * pitch + ix;
-            const float gP = cl_d2(Pc + i, 1) * inv_dh2, gF = cl_d2(Fc + ih, pitch) * inv_dh2;
-            float Gv = gP, Hv = gF;
-            const bool xl = ix < cpml || ix > nx - cpml - 1, zl = iz >= zb;
-            if (xl || zl) {
-                const int ib = (w.lr + kRad) * pitch + ix;
-                const float tx = cl_d1(PSX + i, 1) * inv_dh, tz = cl_d1(PSZ + ib, pitch) * inv_dh;
-                float nzx = 0.f, nzz = 0.f;
-                if (xl) {
-                    nzx = BX[ix] * ZX[i] + AX[ix] * (gP + tx);
-                    ZX[i] = nzx;
-                }
-                if (zl) {
-                    nzz = BZ[w.lr + kRad] * ZZ[i] + AZ[w.lr + kRad] * (gF + tz);
-                    ZZ[i] = nzz;
-                }
-                Gv = gP + (tx + nzx);
-                Hv = gF + (tz + nzz);
+        // 4 columns a thread (16-byte shared loads and stores; the last group of a row may reach
+        // the frame, whose values stay zero)
+        for (int q = threadIdx.x; q < G.nrows * nq; q += blockDim.x) {
+            const int lr = q / nq, ix = 4 + 4 * (q - lr * nq), iz = G.iz0 + lr;
+            const int i = lr * pitch + ix, ih = (lr + kClHalo) * pitch + ix, rb = lr + kRad;
+            const int nval = min(4, nx - 4 - ix);
+            float pw[12], gP[4], gF[4], Gv[4], Hv[4];
+            cl_ld12(pw, Pc + i);
+            cl_d2z4(gF, Fc + ih, pitch);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                gP[j] = cl_d2w(pw, j) * inv_dh2;
+                gF[j] *= inv_dh2;
+                Gv[j] = gP[j];
+                Hv[j] = gF[j];
             }
-            const float mpH = MP[i] * Hv;
-            float vp = VP[i] + (MH[i] * Gv + mpH), vf = VF[i] + (MN[i] * Gv + mpH);
-            if (iz == sh.sz && ix == sh.sx) {
-                vp += wv;
-                vf += wv;
+            const bool zl = iz >= zb;
+            if (zl || ix < cpml || ix + 3 > nx - cpml - 1) {  // a point of the CPML layers
+                // psi_x is zero beyond 4 columns of the side bands, psi_z above 4 rows of the bottom
+                float tx[4] = {0.f, 0.f, 0.f, 0.f}, tz[4] = {0.f, 0.f, 0.f, 0.f};
+                if (ix < cpml + 4 || ix + 3 > nx - cpml - 5) {
+                    float sw[12];
+                    cl_ld12(sw, PSX + i);
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if (ix + j < cpml + 4 || ix + j > nx - cpml - 5) tx[j] = cl_d1w(sw, j) * inv_dh;
+                }
+                if (iz >= zb - 4) {
+                    cl_d1z4(tz, PSZ + rb * pitch + ix, pitch);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) tz[j] *= inv_dh;
+                }
+                float zx[4], zz[4], ax[4], bx[4];
+                cl_ld4(zx, ZX + i);
+                cl_ld4(zz, ZZ + i);
+                cl_ld4(ax, AX + ix);
+                cl_ld4(bx, BX + ix);
+                const float az = AZ[rb], bz = BZ[rb];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const bool xl = ix + j < cpml || ix + j > nx - cpml - 1;
+                    if (j < nval && (xl || zl)) {
+                        float nzx = 0.f, nzz = 0.f;
+                        if (xl) {
+                            nzx = bx[j] * zx[j] + ax[j] * (gP[j] + tx[j]);
+                            zx[j] = nzx;
+                        }
+                        if (zl) {
+                            nzz = bz * zz[j] + az * (gF[j] + tz[j]);
+                            zz[j] = nzz;
+                        }
+                        Gv[j] = gP[j] + (tx[j] + nzx);
+                        Hv[j] = gF[j] + (tz[j] + nzz);
+                    }
+                }
+                cl_st4(ZX + i, zx);
+                cl_st4(ZZ + i, zz);
             }
-            VP[i] = vp;
-            VF[i] = vf;
-            const float nP = Pc[i] + vp, nF = Fc[ih] + vf;
-            Pn[i] = nP;
-            Fn[ih] = nF;
-            if (Cd::scaled) lmax = fmaxf(lmax, fmaxf(fabsf(nP), fabsf(nF)));
-            if (iz == sh.rz) RB[ix] = nP + nF;
+            float mh[4], mp[4], mn[4], vp[4], vf[4], fc[4], nP[4], nF[4];
+            cl_ld4(fc, Fc + ih);
+            cl_ld4(mh, MH + i);
+            cl_ld4(mp, MP + i);
+            cl_ld4(mn, MN + i);
+            cl_ld4(vp, VP + i);
+            cl_ld4(vf, VF + i);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float mpH = mp[j] * Hv[j];
+                vp[j] = vp[j] + (mh[j] * Gv[j] + mpH);
+                vf[j] = vf[j] + (mn[j] * Gv[j] + mpH);
+                if (iz == sh.sz && ix + j == sh.sx) {
+                    vp[j] += wv;
+                    vf[j] += wv;
+                }
+                nP[j] = pw[4 + j] + vp[j];
+                nF[j] = fc[j] + vf[j];
+                if (j >= nval) vp[j] = vf[j] = nP[j] = nF[j] = Gv[j] = Hv[j] = 0.f;
+                if (Cd::scaled) lmax = fmaxf(lmax, fmaxf(fabsf(nP[j]), fabsf(nF[j])));
+            }
+            cl_st4(VP + i, vp);
+            cl_st4(VF + i, vf);
+            cl_st4(Pn + i, nP);
+            cl_st4(Fn + ih, nF);
+            // rows within 8 of the CTA's edges into the neighbours' halo rows
+            if (lr < kClHalo && Fn_up) cl_st4(Fn_up + (G.nup + kClHalo + lr) * pitch + ix, nF);
+            if (lr >= G.nrows - kClHalo && Fn_dn) cl_st4(Fn_dn + (lr - G.nrows + kClHalo) * pitch + ix, nF);
+            if (iz == sh.rz) {
+                const float r4[4] = {nP[0] + nF[0], nP[1] + nF[1], nP[2] + nF[2], nP[3] + nF[3]};
+                cl_st4(RB + ix, r4);
+            }
             if (img) {
-                IMG[w.lr * ip + ix] = Cd::enc_flag(Gv, sc, sat);
-                IMG[(h + w.lr) * ip + ix] = Cd::enc_flag(Hv, sc, sat);
+                cl_st4_img(IMG + lr * ip + ix, Cd::enc_flag(Gv[0], sc, sat), Cd::enc_flag(Gv[1], sc, sat),
+                           Cd::enc_flag(Gv[2], sc, sat), Cd::enc_flag(Gv[3], sc, sat));
+                cl_st4_img(IMG + (h + lr) * ip + ix, Cd::enc_flag(Hv[0], sc, sat), Cd::enc_flag(Hv[1], sc, sat),
+                           Cd::enc_flag(Hv[2], sc, sat), Cd::enc_flag(Hv[3], sc, sat));
             }
         }
         if (sat) atomicOr(b.status, kStatusSaturated);
@@ -389,13 +637,11 @@ k_cluster_fwd(Batch<float> b, int ntb, int h, int pitch, int img)
 
 // Exact adjoint of shot blockIdx.x / ncta with imaging from the image store (slot of each
 // global step), the residual in b.rec; the shot's gradient added into its slot s of b.g (zeroed
-// by the caller).  Each step's images are prefetched into shared memory with cp.async (one
-// step ahead when two staging buffers fit); the imaging of a step runs at the start of the
-// next one and adds into the gradient with fire-and-forget reductions, so that no global
-// memory operation is pending at a cluster barrier.
+// by the caller) with reductions.  Each step's images are prefetched into shared memory with
+// cp.async (one step ahead when two staging buffers fit).
 template <int ST>
 __global__ void __launch_bounds__(kClusterThreads, 1)
-k_cluster_adj(Batch<float> b, int ntb, int h, int pitch, int abuf)
+k_cluster_adj(Batch<float> b, const __grid_constant__ ClRows rows, int ntb, int h, int pitch, int abuf)
 {
     using Cd = Codec<float, ST>;
     using SI = typename Cd::S;
@@ -405,7 +651,7 @@ k_cluster_adj(Batch<float> b, int ntb, int h, int pitch, int abuf)
     const int s = blockIdx.x / ncta;
     const DevShot sh = b.shots[s];
     ClGeom G;
-    G.init((int)cl.block_rank(), ncta, h, pitch, sh.nx, b.nz);
+    G.init((int)cl.block_rank(), ncta, h, pitch, sh.nx, b.nz, rows);
     const int nx = sh.nx, nz = b.nz, cpml = b.cpml;
     const size_t hp = (size_t)(h + 2 * kClHalo) * pitch, bp = (size_t)(h + 2 * kRad) * pitch,
                  op = (size_t)h * pitch;
@@ -445,25 +691,12 @@ k_cluster_adj(Batch<float> b, int ntb, int h, int pitch, int abuf)
     const int zb = nz - cpml;
     const ClBand band(G, zb);
     const int nbx = cpml > 4 ? min(2 * (cpml - 4), G.nxi) : 0;
+    const int nq = (G.nxi + 3) / 4;
     float *const g0 = b.g[0] + (long)s * b.slot, *const g1 = b.g[1] + (long)s * b.slot,
                  *const g2 = b.g[2] + (long)s * b.slot;
     using C = Coef<float>;
     // band membership of a point (x side layers or the bottom layer)
     auto in_band = [&](int ix, int iz) { return ix < cpml || ix > nx - cpml - 1 || iz >= zb; };
-    // imaging of step j from its staged images and lambda of that step (in LP, LF)
-    auto imaging = [&](int j, float inv_sc) {
-        const SI *const Gs = IMG + (j % abuf) * stage, *const Hs = Gs + (long)h * ip;
-        for (ClWalk w(G); w.on(); w.next()) {
-            const int i = w.lr * pitch + w.ix, si = w.lr * ip + w.ix;
-            const long o = (long)(G.iz0 + w.lr) * b.pitch + w.ix;
-            const float lp = LP[i], lf = LF[i];
-            const float Gv = Cd::dec(Gs[si], inv_sc), Hv = Cd::dec(Hs[si], inv_sc);
-            atomicAdd(g0 + o, kk * Gv * lp);
-            atomicAdd(g1 + o, kk * Hv * (lp + lf));
-            atomicAdd(g2 + o, kk * Gv * lf);
-        }
-    };
-    float inv_sc_prev = 1.f;  // image scale of the previous step, inverted
     int cur = 0;  // u of this step in UX0 / UZ0 (cur 0) or UX1 / UZ1; zero before the first step
     for (int j = 0; j < sh.nt; j++) {
         const int m = sh.nt - j;
@@ -471,9 +704,9 @@ k_cluster_adj(Batch<float> b, int ntb, int h, int pitch, int abuf)
         const float inv_sc = Cd::scaled ? 1.f / b.scale[(long)s * b.nt_max + g_img] : 1.f;
         float *const UXc = cur ? UX1 : UX0, *const UZc = cur ? UZ1 : UZ0;
         float *const UXn = cur ? UX0 : UX1, *const UZn = cur ? UZ0 : UZ1;
-        cl_fill_halo(cl, G, UZc);
-        if (j > 0) imaging(j - 1, inv_sc_prev);
-        __syncthreads();  // the buffer of step j - 1 free again
+        float *const UZn_up = G.k > 0 ? cl.map_shared_rank(UZn, G.k - 1) : nullptr;
+        float *const UZn_dn = G.k + 1 < G.ncta ? cl.map_shared_rank(UZn, G.k + 1) : nullptr;
+        // the next staging buffer was last read by the previous step's phase C
         prefetch(j + abuf - 1);
         // Y of the band points: Y' = -D(w) + b Y with w = u at band points, 0 elsewhere; x of the
         // side-band points of the own rows ...
@@ -481,78 +714,164 @@ k_cluster_adj(Batch<float> b, int ntb, int h, int pitch, int abuf)
             const int lr = q / nbx, c = q - lr * nbx;
             const int ix = c < nbx / 2 ? 4 + c : nx - 4 - nbx + c, iz = G.iz0 + lr;
             const int i = lr * pitch + ix;
-            auto wxv = [&](int dx) {
-                const int x2 = ix + dx;
-                return (x2 > 3 && x2 < nx - 4 && in_band(x2, iz)) ? UXc[i + dx] : 0.f;
-            };
-            const float dwx = C::d1_1 * (wxv(1) - wxv(-1)) - C::d1_2 * (wxv(2) - wxv(-2)) +
-                              C::d1_3 * (wxv(3) - wxv(-3)) - C::d1_4 * (wxv(4) - wxv(-4));
+            float dwx;
+            if (iz >= zb || ix < cpml - 4 || ix > nx - cpml + 3) {  // every tap a band point (or frame, 0)
+                dwx = cl_d1(UXc + i, 1);
+            } else {
+                auto wxv = [&](int dx) {
+                    const int x2 = ix + dx;
+                    return (x2 < cpml || x2 > nx - cpml - 1) ? UXc[i + dx] : 0.f;
+                };
+                dwx = cl_d1v(wxv(1), wxv(-1), wxv(2), wxv(-2), wxv(3), wxv(-3), wxv(4), wxv(-4));
+            }
             YX[i] = -(dwx * inv_dh) + BX[ix] * YX[i];
         }
-        // ... z of the bottom-band points of the own rows and 4 either side
-        for (int q = threadIdx.x; q < band.npts; q += blockDim.x) {
-            const int rr = q / G.nxi, r = band.r0 + rr, ix = 4 + q - rr * G.nxi, iz = G.iz0 + r;
+        // ... z of the bottom-band points of the own rows and 4 either side, 4 columns a thread
+        for (int q = threadIdx.x; q < band.nrows * nq; q += blockDim.x) {
+            const int rr = q / nq, r = band.r0 + rr, ix = 4 + 4 * (q - rr * nq), iz = G.iz0 + r;
             const int ib = (r + kRad) * pitch + ix, ih = (r + kClHalo) * pitch + ix;
-            auto wzv = [&](int dz) {
-                const int z2 = iz + dz;
-                return (z2 > 3 && z2 < nz - 4 && in_band(ix, z2)) ? UZc[ih + dz * pitch] : 0.f;
-            };
-            const float dwz = C::d1_1 * (wzv(1) - wzv(-1)) - C::d1_2 * (wzv(2) - wzv(-2)) +
-                              C::d1_3 * (wzv(3) - wzv(-3)) - C::d1_4 * (wzv(4) - wzv(-4));
-            YZ[ib] = -(dwz * inv_dh) + BZ[r + kRad] * YZ[ib];
+            const int nval = min(4, nx - 4 - ix);
+            float dwz[4], yz[4];
+            if (iz >= zb + 4) {  // every tap a band point (or frame, 0)
+                cl_d1z4(dwz, UZc + ih, pitch);
+            } else {  // taps above the bottom layer count only in the side layers
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const bool side = ix + j < cpml || ix + j > nx - cpml - 1;
+                    auto wzv = [&](int dz) { return (side || iz + dz >= zb) ? UZc[ih + dz * pitch + j] : 0.f; };
+                    dwz[j] = cl_d1v(wzv(1), wzv(-1), wzv(2), wzv(-2), wzv(3), wzv(-3), wzv(4), wzv(-4));
+                }
+            }
+            cl_ld4(yz, YZ + ib);
+            const float bz = BZ[r + kRad];
+#pragma unroll
+            for (int j = 0; j < 4; j++) yz[j] = j < nval ? -(dwz[j] * inv_dh) + bz * yz[j] : 0.f;
+            cl_st4(YZ + ib, yz);
         }
         if (abuf == 2) cl_cp_wait<1>();  // this step's images (the next step's may still fly)
         else cl_cp_wait<0>();
         __syncthreads();
+        const SI *const Gs = IMG + (j % abuf) * stage, *const Hs = Gs + (long)h * ip;
         // lambda^m: increments += Dxx(u) - Dx(a Y) (and z), residual at the receivers; then g, h,
         // Z and u of the next step from the new lambda
-        for (ClWalk w(G); w.on(); w.next()) {
-            const int ix = w.ix, iz = G.iz0 + w.lr, i = w.lr * pitch + ix, ih = (w.lr + kClHalo) * pitch + ix;
-            const int rb = w.lr + kRad, ib = rb * pitch + ix;
-            const float dxx = cl_d2(UXc + i, 1) * inv_dh2, dzz = cl_d2(UZc + ih, pitch) * inv_dh2;
-            float wp, wf;
-            if (ix < cpml + 4 || ix > nx - cpml - 5 || iz >= zb - 4) {  // a CPML coefficient within reach
-                auto vx = [&](int dx) { return AX[ix + dx] * YX[i + dx]; };
-                auto vz = [&](int dz) { return AZ[rb + dz] * YZ[ib + dz * pitch]; };
-                const float dvx = C::d1_1 * (vx(1) - vx(-1)) - C::d1_2 * (vx(2) - vx(-2)) +
-                                  C::d1_3 * (vx(3) - vx(-3)) - C::d1_4 * (vx(4) - vx(-4));
-                const float dvz = C::d1_1 * (vz(1) - vz(-1)) - C::d1_2 * (vz(2) - vz(-2)) +
-                                  C::d1_3 * (vz(3) - vz(-3)) - C::d1_4 * (vz(4) - vz(-4));
-                wp = WP[i] + (dxx - dvx * inv_dh);
-                wf = WF[i] + (dzz - dvz * inv_dh);
-            } else {
-                wp = WP[i] + dxx;
-                wf = WF[i] + dzz;
+        for (int q = threadIdx.x; q < G.nrows * nq; q += blockDim.x) {
+            const int lr = q / nq, ix = 4 + 4 * (q - lr * nq), iz = G.iz0 + lr;
+            const int i = lr * pitch + ix, ih = (lr + kClHalo) * pitch + ix, rb = lr + kRad, ib = rb * pitch + ix;
+            const int nval = min(4, nx - 4 - ix);
+            float uw[12], dxx[4], dzz[4], wp[4], wf[4];
+            cl_ld12(uw, UXc + i);
+            cl_d2z4(dzz, UZc + ih, pitch);
+            cl_ld4(wp, WP + i);
+            cl_ld4(wf, WF + i);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                dxx[j] = cl_d2w(uw, j) * inv_dh2;
+                dzz[j] *= inv_dh2;
             }
-            if (iz == sh.rz && ix >= sh.rx0 && ix < sh.rx1) {
-                const float d = b.rec[sh.rec_off + (long)(m - 1) * nrec + ix - sh.rx0];
-                wp += d;
-                wf += d;
+            // a Y . a term only within reach of a CPML coefficient (a = 0 outside the layers)
+            float dvx[4] = {0.f, 0.f, 0.f, 0.f}, dvz[4] = {0.f, 0.f, 0.f, 0.f};
+            if (ix < cpml + 4 || ix + 3 > nx - cpml - 5) {
+                float aw[12], yw[12];
+                cl_ld12(aw, AX + ix);
+                cl_ld12(yw, YX + i);
+#pragma unroll
+                for (int c = 0; c < 12; c++) yw[c] *= aw[c];
+#pragma unroll
+                for (int j = 0; j < 4; j++) dvx[j] = cl_d1w(yw, j);
             }
-            WP[i] = wp;
-            WF[i] = wf;
-            const float lp = LP[i] + wp, lf = LF[i] + wf;
-            LP[i] = lp;
-            LF[i] = lf;
+            if (iz >= zb - 4) {
+                float yv[9][4];
+#pragma unroll
+                for (int dz = -4; dz <= 4; dz++) {
+                    cl_ld4(yv[dz + 4], YZ + ib + dz * pitch);
+                    const float a = AZ[rb + dz];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) yv[dz + 4][j] *= a;
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    dvz[j] = cl_d1v(yv[5][j], yv[3][j], yv[6][j], yv[2][j], yv[7][j], yv[1][j], yv[8][j], yv[0][j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = ix + j;
+                wp[j] = (c < cpml + 4 || c > nx - cpml - 5) ? wp[j] + (dxx[j] - dvx[j] * inv_dh) : wp[j] + dxx[j];
+                wf[j] = iz >= zb - 4 ? wf[j] + (dzz[j] - dvz[j] * inv_dh) : wf[j] + dzz[j];
+                if (iz == sh.rz && c >= sh.rx0 && c < sh.rx1) {
+                    const float d = b.rec[sh.rec_off + (long)(m - 1) * nrec + c - sh.rx0];
+                    wp[j] += d;
+                    wf[j] += d;
+                }
+            }
+            float lp[4], lf[4], gi[4], hi[4];
+            cl_ld4(lp, LP + i);
+            cl_ld4(lf, LF + i);
+            {
+                SI gs[4], hs[4];
+                cl_ld4_img(gs, Gs + lr * ip + ix);
+                cl_ld4_img(hs, Hs + lr * ip + ix);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    gi[j] = Cd::dec(gs[j], inv_sc);
+                    hi[j] = Cd::dec(hs[j], inv_sc);
+                }
+            }
+            float a0[4], a1[4], a2[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (j >= nval) wp[j] = wf[j] = 0.f;
+                lp[j] = lp[j] + wp[j];
+                lf[j] = lf[j] + wf[j];
+                // imaging
+                a0[j] = kk * gi[j] * lp[j];
+                a1[j] = kk * hi[j] * (lp[j] + lf[j]);
+                a2[j] = kk * gi[j] * lf[j];
+            }
+            cl_st4(WP + i, wp);
+            cl_st4(WF + i, wf);
+            cl_st4(LP + i, lp);
+            cl_st4(LF + i, lf);
+            const long o = (long)iz * b.pitch + ix;  // 16-byte aligned: the pitch is a multiple of 32
+            atomicAdd(reinterpret_cast<float4 *>(g0 + o), make_float4(a0[0], a0[1], a0[2], a0[3]));
+            atomicAdd(reinterpret_cast<float4 *>(g1 + o), make_float4(a1[0], a1[1], a1[2], a1[3]));
+            atomicAdd(reinterpret_cast<float4 *>(g2 + o), make_float4(a2[0], a2[1], a2[2], a2[3]));
             // u of the next step: g = v_hor lP + v_nmo lF, h = v_po (lP + lF) (dt^2 folded in)
-            const float gx = MH[i] * lp + MN[i] * lf, hz = MP[i] * (lp + lf);
-            float ux = gx, uzv = hz;
-            if (in_band(ix, iz)) {
-                const float zx = gx + BX[ix] * ZX[i];
-                const float zz = hz + BZ[rb] * ZZ[i];
-                ZX[i] = zx;
-                ZZ[i] = zz;
-                ux = gx + AX[ix] * zx;
-                uzv = hz + AZ[rb] * zz;
+            float mh[4], mp[4], mn[4], ux[4], uz[4];
+            cl_ld4(mh, MH + i);
+            cl_ld4(mp, MP + i);
+            cl_ld4(mn, MN + i);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                ux[j] = mh[j] * lp[j] + mn[j] * lf[j];
+                uz[j] = mp[j] * (lp[j] + lf[j]);
             }
-            UXn[i] = ux;
-            UZn[ih] = uzv;
+            if (iz >= zb || ix < cpml || ix + 3 > nx - cpml - 1) {
+                float zx[4], zz[4], ax[4], bx[4];
+                cl_ld4(zx, ZX + i);
+                cl_ld4(zz, ZZ + i);
+                cl_ld4(ax, AX + ix);
+                cl_ld4(bx, BX + ix);
+                const float az = AZ[rb], bz = BZ[rb];
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (j < nval && in_band(ix + j, iz)) {
+                        const float gx = ux[j], hz = uz[j];
+                        zx[j] = gx + bx[j] * zx[j];
+                        zz[j] = hz + bz * zz[j];
+                        ux[j] = gx + ax[j] * zx[j];
+                        uz[j] = hz + az * zz[j];
+                    }
+                cl_st4(ZX + i, zx);
+                cl_st4(ZZ + i, zz);
+            }
+            cl_st4(UXn + i, ux);
+            cl_st4(UZn + ih, uz);
+            if (lr < kClHalo && UZn_up) cl_st4(UZn_up + (G.nup + kClHalo + lr) * pitch + ix, uz);
+            if (lr >= G.nrows - kClHalo && UZn_dn) cl_st4(UZn_dn + (lr - G.nrows + kClHalo) * pitch + ix, uz);
         }
         cl.sync();  // lambda and u of the next step complete in every CTA
-        inv_sc_prev = inv_sc;
         cur ^= 1;
     }
-    if (sh.nt > 0) imaging(sh.nt - 1, inv_sc_prev);
     cl_cp_wait<0>();  // nothing in flight at exit (an empty group when the prefetch ran past the end)
     cl.sync();  // no CTA leaves while a neighbour may still read its shared memory
 }

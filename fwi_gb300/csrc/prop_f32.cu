@@ -259,12 +259,36 @@ size_t cluster_smem_limit()
 
 int store_elem_bytes(int store_type) { return store_type == kStoreNative ? (int)sizeof(float) : 2; }
 
+// The cluster plan of a window width, grid height, layer width and image type, made once (the
+// partition is a small dynamic programme) and kept for the process.
+bool cached_cluster_plan(int nx, int nz, int cpml, int store_type, ClusterPlan &p)
+{
+    struct Entry {
+        int nx, nz, cpml, st;
+        bool ok;
+        ClusterPlan p;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Entry &e : cache)
+        if (e.nx == nx && e.nz == nz && e.cpml == cpml && e.st == store_type) {
+            p = e.p;
+            return e.ok;
+        }
+    Entry e{nx, nz, cpml, store_type, false, {}};
+    e.ok = cluster_plan(nx, nz, cpml, store_elem_bytes(store_type), cluster_smem_limit(), e.p);
+    cache.push_back(e);
+    p = e.p;
+    return e.ok;
+}
+
 }  // namespace
 
-bool cluster_shot_fits(int nx_max, int nz, int store_type)
+bool cluster_shot_fits(int nx_max, int nz, int cpml, int store_type)
 {
     ClusterPlan p;
-    if (!cluster_plan(nx_max, nz, store_elem_bytes(store_type), cluster_smem_limit(), p)) return false;
+    if (!cached_cluster_plan(nx_max, nz, cpml, store_type, p)) return false;
     // every kernel may take the device's whole opt-in shared memory: one setting serves all widths
     const size_t lim = cluster_smem_limit();
     for (cudaError_t e : {cluster_attrs(k_cluster_fwd<kStoreNative>, lim), cluster_attrs(k_cluster_fwd<kStoreHalf>, lim),
@@ -297,28 +321,26 @@ bool cluster_shot_fits(int nx_max, int nz, int store_type)
 cudaError_t launch_cluster_forward(const Batch<float> &b, int nx_max, int ntb, bool images, cudaStream_t st)
 {
     ClusterPlan p;
-    if (!cluster_plan(nx_max, b.nz, store_elem_bytes(b.store_type), cluster_smem_limit(), p))
-        return cudaErrorInvalidValue;
+    if (!cached_cluster_plan(nx_max, b.nz, b.cpml, b.store_type, p)) return cudaErrorInvalidValue;
     const int img = images ? 1 : 0, n = p.ncta;
     const size_t sm = p.smem_fwd;
     switch (b.store_type) {
-    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, n, b.B, sm, st, b, ntb, p.h, p.pitch, img);
-    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, n, b.B, sm, st, b, ntb, p.h, p.pitch, img);
-    default: return cluster_launch(k_cluster_fwd<kStoreNative>, n, b.B, sm, st, b, ntb, p.h, p.pitch, img);
+    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, img);
+    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, img);
+    default: return cluster_launch(k_cluster_fwd<kStoreNative>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, img);
     }
 }
 
 cudaError_t launch_cluster_adjoint(const Batch<float> &b, int nx_max, int ntb, cudaStream_t st)
 {
     ClusterPlan p;
-    if (!cluster_plan(nx_max, b.nz, store_elem_bytes(b.store_type), cluster_smem_limit(), p))
-        return cudaErrorInvalidValue;
+    if (!cached_cluster_plan(nx_max, b.nz, b.cpml, b.store_type, p)) return cudaErrorInvalidValue;
     const int n = p.ncta, ab = p.abuf;
     const size_t sm = p.smem_adj;
     switch (b.store_type) {
-    case kStoreHalf: return cluster_launch(k_cluster_adj<kStoreHalf>, n, b.B, sm, st, b, ntb, p.h, p.pitch, ab);
-    case kStoreBf16: return cluster_launch(k_cluster_adj<kStoreBf16>, n, b.B, sm, st, b, ntb, p.h, p.pitch, ab);
-    default: return cluster_launch(k_cluster_adj<kStoreNative>, n, b.B, sm, st, b, ntb, p.h, p.pitch, ab);
+    case kStoreHalf: return cluster_launch(k_cluster_adj<kStoreHalf>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, ab);
+    case kStoreBf16: return cluster_launch(k_cluster_adj<kStoreBf16>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, ab);
+    default: return cluster_launch(k_cluster_adj<kStoreNative>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, ab);
     }
 }
 
