@@ -325,6 +325,9 @@ def native_arm(args, rank, world, dist):
             r["clocks"] = clk
         return r
 
+    if args.only_accuracy:  # the FP64 comparison alone (any storage, large workloads)
+        return {"metric": METRIC, "workload": w.name, "shots": nshots, "storage": args.storage,
+                "accuracy_vs_fp64": accuracy(args, w, context, obs_d, fwi_gb300)} if rank == 0 else None
     if args.only_inversion:  # the inversion loop alone (large workloads)
         return {"metric": METRIC, "workload": w.name, "shots": nshots, "storage": args.storage,
                 "inversion": inversion(args, w, context, obs_d, shots, torch)} if rank == 0 else None
@@ -363,6 +366,7 @@ def native_arm(args, rank, world, dist):
         sub = fwi_gb300.make_shots(w.shots[: args.plain_shots])
         nsub = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots[: args.plain_shots])
         plain = {}
+        os.environ["FWI_CLUSTER"] = "0"  # the per-step tile launches, whatever the window
         for graphs in (False, True):
             c1 = context(1, store_prec=fwi_gb300.SPREC_NATIVE, store="full")
             c1.set_graphs(graphs)
@@ -375,6 +379,7 @@ def native_arm(args, rank, world, dist):
             torch.cuda.synchronize()
             plain[graphs] = args.plain_shots / (time.perf_counter() - t0)
             del c1
+        os.environ.pop("FWI_CLUSTER", None)
         value = out["value"] / world
         out["plain_gpu"] = {"value": round(plain[False], 4), "unit": "shots/s",
                             "how": f"max_shots=1, FP32 images, full storage, kernels launched from the host "
@@ -385,6 +390,7 @@ def native_arm(args, rank, world, dist):
         for k, o in out.get("other_storage", {}).items():
             o["plain_gpu_speedup"] = round(o["value"] / world / plain[False], 2)
         out["accuracy_vs_fp64"] = accuracy(args, w, context, obs_d, fwi_gb300)
+        out["single_shot_c1"] = single_shot_c1(args, fwi_gb300, torch, dev)
         # L-BFGS two-loop (m = 5) on this grid, FP64 dots
         cl = context(1)
         cl.set_model(*w.squared(initial=True))
@@ -414,6 +420,56 @@ def native_arm(args, rank, world, dist):
     return out
 
 
+def single_shot_c1(args, fwi_gb300, torch, dev, steps=10, warmup=3):
+    """The plain single-shot gradient (C1: 209 x 209, nt 2000, one shot, full image storage) on the
+    small-shot cluster path (one 16-CTA cluster takes the shot through every step in one launch per
+    phase) and, beside it, on the per-step tile passes (FWI_CLUSTER=0); device-resident inputs,
+    CUDA events over `steps` gradients after `warmup`."""
+    from fwi_gb300 import synth
+    w = synth.WORKLOADS["C1"]()
+    shots = fwi_gb300.make_shots(w.shots)
+    sprec = {"fp32": fwi_gb300.SPREC_NATIVE, "fp16": fwi_gb300.SPREC_FP16, "bf16": fwi_gb300.SPREC_BF16}[args.store]
+    out = {"workload": w.name, "storage": "full", "image_store": args.store, "steps": steps}
+    obs = None
+    for name, flag in (("cluster", "1"), ("tile_passes", "0")):
+        os.environ["FWI_CLUSTER"] = flag
+        c = fwi_gb300.Context(nx=w.nx, nz=w.nz, dh=w.dh, dt=w.dt, cpml=w.cpml, f_cpml=w.f, nt_max=w.nt,
+                              max_shots=1, max_receivers=w.nx, mode=fwi_gb300.MODE_EXACT,
+                              precision=fwi_gb300.PREC_FP32, store_prec=sprec, store=fwi_gb300.STORE_FULL,
+                              device=dev)
+        c.set_ricker(w.f, w.nt)
+        if obs is None:
+            c.set_model(*w.squared())
+            obs = torch.zeros(w.nt * (w.shots[0]["rx1"] - w.shots[0]["rx0"]), dtype=torch.float32, device="cuda")
+            c.forward(shots, out=obs)
+        c.set_model(*w.squared(initial=True))
+        g = [torch.zeros((w.nz, w.nx), dtype=torch.float32, device="cuda") for _ in range(3)]
+        for _ in range(warmup):
+            c.gradient(shots, obs, out=g)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        t_fwd = t_adj = 0.0
+        launches = 0
+        for _ in range(steps):
+            c.gradient(shots, obs, out=g)
+            t = c.last_timing()
+            t_fwd += float(t[1])
+            t_adj += float(t[2])
+            launches += c.last_launches()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"value": round(1e3 / ms, 3), "unit": "shots/s", "ms_per_gradient": round(ms, 3),
+                     "phase_ms": {"forward": round(t_fwd / steps, 3), "adjoint": round(t_adj / steps, 3)},
+                     "launches_per_gradient": launches // steps,
+                     "gpt_updates_per_s": round(w.physical_point_updates() / (ms / 1e3) / 1e9, 3)}
+        del c
+    os.environ.pop("FWI_CLUSTER", None)
+    out["cluster_speedup_over_tile_passes"] = round(out["cluster"]["value"] / out["tile_passes"]["value"], 3)
+    return out
+
+
 def accuracy(args, w, context, obs_d, fwi_gb300):
     """Residual, misfit and gradient errors of this configuration (storage, image type) against the FP64 GPU
     path on the first shots, same observed data.  Gradients compare over the whole grid and over the rows
@@ -423,17 +479,22 @@ def accuracy(args, w, context, obs_d, fwi_gb300):
     nsub = sum(s["nt"] * (s["rx1"] - s["rx0"]) for s in w.shots[:n])
     obs32 = obs_d[:nsub].cpu().numpy()
     mask = None if w.mask is None else w.mask[: sum(s["rx1"] - s["rx0"] for s in w.shots[:n])]
-    c64 = context(min(n, args.batch), precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE,
-                  store="full")
+    # every step's images kept where they fit (60 GB), else checkpoints (the same images, recomputed)
+    nb = min(n, args.batch)
+    win = max((s["nxw"] or w.nx) for s in w.shots[:n])
+    full_bytes = lambda elem: nb * w.nt * 2 * w.nz * (-(-win // 32) * 32) * elem
+    ref_store = "full" if full_bytes(8) <= 60e9 else "checkpoint"
+    c64 = context(nb, precision=fwi_gb300.PREC_FP64, store_prec=fwi_gb300.SPREC_NATIVE, store=ref_store)
     c64.set_model(*(a.astype(np.float64) for a in w.squared(initial=True)))
     r64 = c64.gradient(sub, obs32.astype(np.float64), mask)
     syn64 = c64.forward(sub)
     del c64
-    out = {"shots": n, "order": "v_hor, v_po, v_nmo", "update_rows": "iz > 15"}
+    out = {"shots": n, "order": "v_hor, v_po, v_nmo", "update_rows": "iz > 15", "fp64_storage": ref_store}
     rel = lambda a, b, z=0: float(np.linalg.norm((a - b)[z:]) / np.linalg.norm(b[z:]))
     res64 = syn64 - obs32.astype(np.float64)
+    exact32 = "full" if full_bytes(4) <= 60e9 else "checkpoint"
     for label, store, sp in ((f"{args.storage}_{args.store}", args.storage, None),
-                             ("full_fp32_images", "full", fwi_gb300.SPREC_NATIVE)):
+                             (f"{exact32}_fp32_images", exact32, fwi_gb300.SPREC_NATIVE)):
         cx = context(min(n, args.batch), store=store, **({} if sp is None else {"store_prec": sp}))
         cx.set_model(*w.squared(initial=True))
         rx = cx.gradient(sub, obs32, mask)
@@ -561,6 +622,8 @@ def main():
     ap.add_argument("--accuracy-shots", type=int, default=8, help="shots of the FP64 comparison")
     ap.add_argument("--invert-iters", type=int, default=20,
                     help="L-BFGS iterations of the timed inversion loop (per band for multiscale workloads; 0: none)")
+    ap.add_argument("--only-accuracy", action="store_true",
+                    help="only the FP64 comparison of --storage / --store on --accuracy-shots shots")
     ap.add_argument("--only-inversion", action="store_true",
                     help="time the inversion loop only (no gradient benchmark), e.g. C5's bands on a shot subset")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -27,3 +27,13 @@ def pytest_collection_modifyitems(config, items):
     for item in items:
         if "gpu" in item.keywords:
             item.add_marker(skip)
+
+
+@pytest.fixture
+def tile_path(monkeypatch):
+    """The per-step tile passes for every window (FWI_CLUSTER=0): tests of properties the tile
+    passes hold between storage modes, launch groupings and graph replay, which the small-shot
+    cluster path (one launch per phase, full storage only, another summation order) does not
+    share bit for bit."""
+    monkeypatch.setenv("FWI_CLUSTER", "0")
+    yield

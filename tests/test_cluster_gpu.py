@@ -76,3 +76,36 @@ def test_cluster_path_reduced_precision_images(case, sprec, tol, monkeypatch):
     assert Jc == J32  # the images do not enter the misfit
     for a, b, c in zip(gc, gt, g32):
         assert rel(a, c) <= tol and rel(a, b) <= tol
+
+
+@pytest.fixture(scope="module")
+def c1_case():
+    """A C1-sized grid (209 x 209, 20-point layer): 16 CTAs of unequal rows (fewer at the
+    bottom layer), one image buffer for FP32 images and two for FP16 in the adjoint."""
+    p = exact_problem(seed=5, nx=209, nz=209, nt=240)
+    p["cpml"] = 20
+    nx, nz = p["nx"], p["nz"]
+    shots = [dict(sx=104, sz=6, rz=6, rx0=4, rx1=nx - 4, nt=p["nt"], x0=0, nxw=0)]
+    from fwi_gb300 import Context, MODE_EXACT, PREC_FP64, make_shots
+    ctx = Context(nx=nx, nz=nz, dh=p["dh"], dt=p["dt"], cpml=p["cpml"], f_cpml=p["f"], nt_max=p["nt"], max_shots=1,
+                  mode=MODE_EXACT, precision=PREC_FP64)
+    ctx.set_wavelet(wavelet(p))
+    ctx.set_model(p["vh"] * 1.03, p["vp"] * 0.98, p["vn"] * 1.02)
+    obs = ctx.forward(make_shots(shots))
+    mask = np.ones(nx - 8, np.uint8)
+    J, g = oracle_exact(p, shots, obs, mask)
+    return p, shots, obs, mask, J, g
+
+
+@pytest.mark.parametrize("sprec,tol_tile", [(0, 1e-5), (1, 2e-3)])
+def test_cluster_path_c1_grid_unequal_rows(c1_case, sprec, tol_tile, monkeypatch):
+    p, shots, obs, mask, J, g = c1_case
+    (Jc, *gc), lc, _ = run(p, shots, obs, mask, sprec=sprec)
+    (Jt, *gt), lt, _ = run(p, shots, obs, mask, sprec=sprec, cluster=False, monkeypatch=monkeypatch)
+    e_or = [rel(a, b) for a, b in zip(gc, g)]
+    e_tile = [rel(a, b) for a, b in zip(gc, gt)]
+    print(f"[parity] cluster path, 209 x 209, images {sprec}: vs FP64 oracle {max(e_or):.3e}, vs tile passes "
+          f"{max(e_tile):.3e}; launches {lc} vs {lt}")
+    assert lc < 10 < lt
+    assert abs(Jc - J) <= 1e-5 * J and abs(Jc - Jt) <= 1e-6 * Jt
+    assert max(e_tile) <= tol_tile and max(e_or) <= (1e-4 if sprec == 0 else tol_tile)

@@ -289,6 +289,7 @@ def test_errors_are_reported_not_faulted():
 @pytest.mark.parametrize("mode", ["exact", "ref"])
 @pytest.mark.parametrize("every,sprec", [(1, 0), (37, 0), (64, 1), (0, 2), (260, 0)])
 @pytest.mark.parametrize("batch", [2, 1])
+@pytest.mark.usefixtures("tile_path")
 def test_checkpointing_reproduces_full_storage_bitwise(exact_case, mode, every, sprec, batch):
     """Segments recomputed from checkpoints give the images a full store keeps,
     so the gradient is bit-identical (uneven nt and windows included; batch 1
@@ -322,6 +323,7 @@ def rebuild_region_mask(p, shots):
 
 @pytest.mark.parametrize("precision,sprec,tol", [("fp64", 0, 1e-9), ("fp32", 0, 2e-4), ("fp32", 1, 2e-3)])
 @pytest.mark.parametrize("mode", ["exact", "ref"])
+@pytest.mark.usefixtures("tile_path")
 def test_boundary_storage_rebuilds_the_images(exact_case, precision, sprec, tol, mode):
     """FWI_STORE_BOUNDARY: the misfit is the full store's exactly; inside the
     region every shot rebuilds, the gradient is the full store's up to the
@@ -350,6 +352,7 @@ def test_boundary_storage_rebuilds_the_images(exact_case, precision, sprec, tol,
 
 @pytest.mark.parametrize("store", ["full", "checkpoint", "boundary"])
 @pytest.mark.parametrize("batch", [2, 1])
+@pytest.mark.usefixtures("tile_path")
 def test_graph_replay_matches_direct_issue_bitwise(exact_case, store, batch):
     """Batch sections replayed as CUDA graphs (captured on the second call with
     the same launch parameters) give the results of direct issue bit for bit,
@@ -432,6 +435,7 @@ def test_edge_geometries_match_fp64_oracle(case):
 
 
 @pytest.mark.parametrize("store", ["full", "checkpoint", "boundary"])
+@pytest.mark.usefixtures("tile_path")
 def test_groups_of_several_windows_are_bitwise_one_shot_per_block(exact_case, store):
     """The interior passes' groups of several windows (MIXED kernels: per-shot
     tile roles, model columns and gradient slots) give the results of one
