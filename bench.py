@@ -257,6 +257,7 @@ def native_arm(args, rank, world, dist):
         launches = 0
         t_fwd = t_adj = t_tot = 0.0
         tile = np.zeros(4)
+        rec = np.zeros(3)
         e0.record()
         for _ in range(args.steps):
             J = step()
@@ -265,6 +266,7 @@ def native_arm(args, rank, world, dist):
             t_fwd += float(t[1])
             t_adj += float(t[2])
             tile += ctx.last_tile_timing() / args.steps
+            rec += ctx.last_recompute_timing() / args.steps
             launches += ctx.last_launches()
         e1.record()
         torch.cuda.synchronize()
@@ -286,30 +288,57 @@ def native_arm(args, rank, world, dist):
         ms_e2e = max_over_ranks(dist, (time.perf_counter() - t0) * 1e3 / args.steps)
         barrier(dist)
         del ctx
-        # dominant kernel: the adjoint interior tiles (the largest share of the launch list); per launch:
-        # algorithmic bytes of the interior points it updates / its mean duration, from CUDA events on its
-        # stream around sampled launches
+        # dominant kernel: of the two interior tile passes, the one with the larger live total (mean
+        # sampled launch duration x launches): the adjoint's with full storage; the forward's with
+        # checkpoint storage, where it runs twice (the forward, and each segment's recompute beside the
+        # adjoint).  Per launch: algorithmic bytes of the interior points it updates / its mean duration,
+        # from CUDA events on its stream around sampled launches
         adj_ms, adj_pts = float(tile[2]), float(tile[3])
         fwd_ms, fwd_pts = float(tile[0]), float(tile[1])
+        rec_ms, rec_pts, rec_steps = float(rec[0]), float(rec[1]), float(rec[2])
+        batches = [w.shots[i:i + args.batch] for i in range(0, nshots, args.batch)]
+        steps_fwd = sum(max(s["nt"] for s in bt) for bt in batches)  # interior launches of a phase
+        fwd_launches = steps_fwd + rec_steps
+        fwd_mean = (fwd_ms * steps_fwd + rec_ms * rec_steps) / fwd_launches if fwd_launches else 0.0
         kern_gbs = adj_bytes * adj_pts / (adj_ms / 1e3) / 1e9 if adj_ms > 0 else None
-        fwd_kern_gbs = ALG_BYTES_FWD * fwd_pts / (fwd_ms / 1e3) / 1e9 if fwd_ms > 0 else None
+        fwd_kern_gbs = ALG_BYTES_FWD * fwd_pts / (fwd_mean / 1e3) / 1e9 if fwd_mean > 0 else None
+        fwd_dominant = fwd_mean * fwd_launches > adj_ms * steps_fwd
+        img_write = adj_bytes - (ALG_BYTES_ADJ - 8)  # the two images of a point: 4 B in FP16, 8 B in FP32
+        rec_bytes = (ALG_BYTES_FWD + img_write) * rec_pts * rec_steps
         r = {
             "value": round(world * nshots / (ms / 1e3), 4), "ms_per_step": round(ms, 3), "misfit": J,
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
                     "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
-            "roofline": {"bound": "hbm", "kernel": "k_adj_tma interior tiles (adjoint step + imaging)",
-                         "achieved": round(kern_gbs, 1) if kern_gbs else None, "peak": hbm, "unit": "GB/s",
-                         "frac": round(kern_gbs / hbm, 4) if kern_gbs else None, "peak_kind": peak_kind,
-                         "traffic": traffic_from_profile(f"k_adj_tma_interior_{args.workload}.txt"),
-                         "launch_ms": round(adj_ms, 4), "points_per_launch": int(adj_pts),
-                         "bytes_per_point": adj_bytes,
-                         "forward_interior": {"achieved": round(fwd_kern_gbs, 1) if fwd_kern_gbs else None,
-                                              "frac": round(fwd_kern_gbs / hbm, 4) if fwd_kern_gbs else None,
-                                              "launch_ms": round(fwd_ms, 4), "points_per_launch": int(fwd_pts),
-                                              "bytes_per_point": ALG_BYTES_FWD},
-                         # whole phases (all kernels of a step, every updated point), on the context stream
+            "roofline": ({"bound": "hbm", "kernel": "k_fwd_tma interior tiles (forward step; with checkpoint "
+                                                              "storage also each segment's recompute)",
+                          "achieved": round(fwd_kern_gbs, 1) if fwd_kern_gbs else None, "peak": hbm, "unit": "GB/s",
+                          "frac": round(fwd_kern_gbs / hbm, 4) if fwd_kern_gbs else None, "peak_kind": peak_kind,
+                          "traffic": traffic_from_profile(f"k_fwd_tma_interior_{args.workload}.txt"),
+                          "launch_ms": round(fwd_mean, 4), "points_per_launch": int(fwd_pts),
+                          "bytes_per_point": ALG_BYTES_FWD,
+                          "launches_per_gradient": int(fwd_launches),
+                          "forward_pass_launch_ms": round(fwd_ms, 4), "recompute_launch_ms": round(rec_ms, 4),
+                          "adjoint_interior": {"achieved": round(kern_gbs, 1) if kern_gbs else None,
+                                               "frac": round(kern_gbs / hbm, 4) if kern_gbs else None,
+                                               "launch_ms": round(adj_ms, 4), "points_per_launch": int(adj_pts),
+                                               "bytes_per_point": adj_bytes}}
+                         if fwd_dominant else
+                         {"bound": "hbm", "kernel": "k_adj_tma interior tiles (adjoint step + imaging)",
+                          "achieved": round(kern_gbs, 1) if kern_gbs else None, "peak": hbm, "unit": "GB/s",
+                          "frac": round(kern_gbs / hbm, 4) if kern_gbs else None, "peak_kind": peak_kind,
+                          "traffic": traffic_from_profile(f"k_adj_tma_interior_{args.workload}.txt"),
+                          "launch_ms": round(adj_ms, 4), "points_per_launch": int(adj_pts),
+                          "bytes_per_point": adj_bytes, "launches_per_gradient": int(steps_fwd),
+                          "forward_interior": {"achieved": round(fwd_kern_gbs, 1) if fwd_kern_gbs else None,
+                                               "frac": round(fwd_kern_gbs / hbm, 4) if fwd_kern_gbs else None,
+                                               "launch_ms": round(fwd_mean, 4), "points_per_launch": int(fwd_pts),
+                                               "bytes_per_point": ALG_BYTES_FWD}}) | {
+                         # whole phases (all kernels of a step, every updated point), on the context stream;
+                         # the adjoint phase with checkpoint storage also carries the segment recompute
                          "adjoint_step_frac": round(adj_bytes * pts / (t_adj / args.steps / 1e3) / 1e9 / hbm, 4),
+                         "adjoint_phase_frac_with_recompute": round((adj_bytes * pts + rec_bytes)
+                                                                    / (t_adj / args.steps / 1e3) / 1e9 / hbm, 4),
                          "forward_step_frac": round(ALG_BYTES_FWD * pts / (t_fwd / args.steps / 1e3) / 1e9 / hbm, 4),
                          # the survey's point-update basis: useful updates x 52 B (36 + 68, two updates)
                          "gradient_frac": round(world * upd / (ms / 1e3) * (ALG_BYTES_FWD + ALG_BYTES_ADJ) / 2

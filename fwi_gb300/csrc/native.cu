@@ -544,12 +544,16 @@ struct CtxBase {
 
     // Interior tile timing (fwi_set_tile_timing): event pairs around the
     // interior tile launches of up to kTimeSamples sampled steps per phase
-    // (0 forward, 1 adjoint), with the interior points each launch updated.
+    // (0 forward, 1 adjoint, 2 the forward steps of a checkpoint segment's
+    // recompute, which run beside the adjoint), with the interior points each
+    // launch updated; recompute_steps: forward steps the last call recomputed.
     static constexpr int kTimeSamples = 16;
+    static constexpr int kPhases = 3;
     bool tile_timing = false;
-    cudaEvent_t tev[2][kTimeSamples][2] = {};
-    double tile_ms[2] = {0, 0}, tile_pts[2] = {0, 0};
-    long tile_n[2] = {0, 0};
+    cudaEvent_t tev[kPhases][kTimeSamples][2] = {};
+    double tile_ms[kPhases] = {0, 0, 0}, tile_pts[kPhases] = {0, 0, 0};
+    long tile_n[kPhases] = {0, 0, 0};
+    long recompute_steps = 0;
     // CUDA graphs of the batch sections (Ctx<T>::run_section): on/off, sections
     // replayed and captured
     bool graphs = true;
@@ -681,8 +685,10 @@ template <typename T> struct Ctx : CtxBase {
         std::vector<long> key;
         cudaGraphExec_t exec = nullptr;
         long launches = 0;              // kernel launches of the section
-        int phase = 0, nsamp = 0;       // tile timing samples it takes (phase, count, points)
-        double spts[kTimeSamples] = {};
+        unsigned phases = 0;            // tile timing phases it samples (bit p: phase p) ...
+        int nsamp[kPhases] = {};        // ... their sample counts and points
+        double spts[kPhases][kTimeSamples] = {};
+        long rsteps = 0;                // forward steps of segment recomputes it runs
         unsigned long long used = 0;
     };
     static constexpr int kSections = 6;
@@ -729,10 +735,11 @@ template <typename T> struct Ctx : CtxBase {
 
     // Issues `body` (launches on st and on streams it joins back into st) as
     // the section `key`: directly, or captured into a graph, or by replaying
-    // the graph.  The section's host bookkeeping (launch count, timing
-    // samples of `phase`: nsamp[phase] and the points row `spts`) is kept
-    // with it for the replays.
-    template <typename F> int run_section(const std::vector<long> &key, int phase, int *nsamp, double *spts, F body)
+    // the graph.  The section's host bookkeeping (launch count, recomputed
+    // steps, timing samples of the phases in the mask `phases`: nsamp[p] and
+    // the points rows spts[p]) is kept with it for the replays.
+    template <typename F>
+    int run_section(const std::vector<long> &key, unsigned phases, int *nsamp, double (*spts)[kTimeSamples], F body)
     {
         Section *s = nullptr;
         for (Section &c : sections)
@@ -741,8 +748,12 @@ template <typename T> struct Ctx : CtxBase {
             s->used = ++section_clock;
             TRY(cudaGraphLaunch(s->exec, st));
             launches += s->launches;
-            nsamp[phase] = s->nsamp;
-            std::copy(s->spts, s->spts + kTimeSamples, spts);
+            recompute_steps += s->rsteps;
+            for (int p = 0; p < kPhases; p++)
+                if (phases >> p & 1) {
+                    nsamp[p] = s->nsamp[p];
+                    std::copy(s->spts[p], s->spts[p] + kTimeSamples, spts[p]);
+                }
             graph_replays++;
             return FWI_OK;
         }
@@ -759,8 +770,8 @@ template <typename T> struct Ctx : CtxBase {
             s->key = key;
         }
         s->used = ++section_clock;
-        s->phase = phase;
-        const long l0 = launches;
+        s->phases = phases;
+        const long l0 = launches, r0 = recompute_steps;
         if (capture) TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         const int rc = body();
         if (capture) {
@@ -779,8 +790,12 @@ template <typename T> struct Ctx : CtxBase {
         }
         if (rc != FWI_OK) return rc;
         s->launches = launches - l0;
-        s->nsamp = nsamp[phase];
-        std::copy(spts, spts + kTimeSamples, s->spts);
+        s->rsteps = recompute_steps - r0;
+        for (int p = 0; p < kPhases; p++)
+            if (phases >> p & 1) {
+                s->nsamp[p] = nsamp[p];
+                std::copy(spts[p], spts[p] + kTimeSamples, s->spts[p]);
+            }
         return FWI_OK;
     }
     float *scale = nullptr, *amax = nullptr;
@@ -1377,7 +1392,8 @@ template <typename T> struct Ctx : CtxBase {
         if (rc) return rc;
         TRY(cudaEventRecord(ev[0], st));
         long launches0 = launches;
-        for (int p = 0; p < 2; p++) { tile_ms[p] = tile_pts[p] = 0; tile_n[p] = 0; }
+        for (int p = 0; p < kPhases; p++) { tile_ms[p] = tile_pts[p] = 0; tile_n[p] = 0; }
+        recompute_steps = 0;
         const long kps = sizeof(T) == 4 ? 3 : 2;  // kernels per time step (see the file comment)
         if (want_grad)
             for (auto &p : grad) TRY(cudaMemsetAsync(p, 0, mslot * sizeof(T), st));
@@ -1433,14 +1449,15 @@ template <typename T> struct Ctx : CtxBase {
             // sampled steps of the interior tile timing: events and interior points updated
             const bool timed = tile_timing && sizeof(T) == 4;
             const int tstride = std::max(1, ntb / kTimeSamples);
-            int nsamp[2] = {0, 0};
-            double spts[2][kTimeSamples] = {};
+            int nsamp[kPhases] = {0, 0, 0};
+            double spts[kPhases][kTimeSamples] = {};
             auto sample = [&](int phase, int step, fwi::StepStreams &sst) {
                 if (!timed || step % tstride != tstride / 2 || nsamp[phase] >= kTimeSamples) return;
-                const int aw = phase == 0 || !exact ? cfg.cpml : cfg.cpml + fwi::kRad;
+                const bool fwd = phase != 1;  // forward steps: the forward and the recompute
+                const int aw = fwd || !exact ? cfg.cpml : cfg.cpml + fwi::kRad;
                 double pts = 0;
                 for (const DevShot &d : bs)
-                    if (phase == 0 ? step - (ntb - d.nt) >= 0 : step < d.nt)
+                    if (fwd ? step - (ntb - d.nt) >= 0 : step < d.nt)
                         pts += (double)interior_tile_points(d.nx, aw, b.xbase, b.zbase);
                 const int k = nsamp[phase]++;
                 spts[phase][k] = pts;
@@ -1481,7 +1498,7 @@ template <typename T> struct Ctx : CtxBase {
                     launches++;
                 }
             }
-            rc = on_cluster ? FWI_OK : run_section(section_key(0), 0, nsamp, spts[0], [&]() -> int {
+            rc = on_cluster ? FWI_OK : run_section(section_key(0), 1u, nsamp, spts, [&]() -> int {
                 int cur = 0;
                 for (int g = 0; g < ntb; g++) {
                     if (ckpt && g % ck_every == 0 && g / ck_every < first_direct) {
@@ -1531,7 +1548,7 @@ template <typename T> struct Ctx : CtxBase {
                 launches += 2;
             } else if (want_grad) {
                 NvtxRange adj_range("fwi adjoint steps + imaging");
-                rc = run_section(section_key(1), 1, nsamp, spts[1], [&]() -> int {
+                rc = run_section(section_key(1), 6u, nsamp, spts, [&]() -> int {
                     for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
                     for (auto &p : cp) TRY(cudaMemsetAsync(p, 0, lb, st));
                     for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
@@ -1615,11 +1632,14 @@ template <typename T> struct Ctx : CtxBase {
                             int rc2 = restore_checkpoint(seg, nb, rcur, rst);
                             if (rc2) return rc2;
                             for (int g = a; g < e; g++) {
-                                fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, (g - a) + h * ck_every, exact, rss);
+                                fwi::StepStreams rsst = rss;
+                                sample(2, g, rsst);
+                                fwi::launch_forward_step<T>(rb, nxm, g, ntb, rcur, (g - a) + h * ck_every, exact, rsst);
                                 rcur ^= 1;
                             }
                             TRY(cudaEventRecord(ev_reb[h], rst));
                             launches += kps * (e - a);
+                            recompute_steps += e - a;
                             return FWI_OK;
                         };
                         // segments first_direct .. last_seg were imaged by the forward itself
@@ -1665,7 +1685,7 @@ template <typename T> struct Ctx : CtxBase {
             cudaEventElapsedTime(&c, e1, e2);
             t_fwd += a;
             t_adj += c;
-            for (int p = 0; p < 2; p++)
+            for (int p = 0; p < kPhases; p++)
                 for (int k = 0; k < nsamp[p]; k++) {
                     float ms = 0;
                     TRY(cudaEventElapsedTime(&ms, tev[p][k][0], tev[p][k][1]));
@@ -2469,6 +2489,17 @@ int fwi_last_tile_timing(void *ctx, double *out4)
         out4[2 * p] = n ? c->tile_ms[p] / n : 0.0;
         out4[2 * p + 1] = n ? c->tile_pts[p] / n : 0.0;
     }
+    return FWI_OK;
+}
+
+int fwi_last_recompute_timing(void *ctx, double *out3)
+{
+    if (!ctx || !out3) return FWI_ERR_ARG;
+    CtxBase *c = as_ctx(ctx);
+    const long n = c->tile_n[2];
+    out3[0] = n ? c->tile_ms[2] / n : 0.0;
+    out3[1] = n ? c->tile_pts[2] / n : 0.0;
+    out3[2] = (double)c->recompute_steps;
     return FWI_OK;
 }
 

@@ -124,6 +124,7 @@ def lib() -> C.CDLL:
         _sig(L, "fwi_last_timing", [_p, _p])
         _sig(L, "fwi_set_tile_timing", [_p, _i])
         _sig(L, "fwi_last_tile_timing", [_p, _p])
+        _sig(L, "fwi_last_recompute_timing", [_p, _p])
         _sig(L, "fwi_last_launches", [_p], _l)
         _sig(L, "fwi_autotune", [_p, shotp, _i, _i, C.POINTER(Tuning)])
         _sig(L, "fwi_set_tuning", [_p, shotp, _i, C.POINTER(Tuning)])
@@ -486,4 +487,11 @@ class Context:
         """(forward ms, forward points, adjoint ms, adjoint points) per interior tile launch."""
         t = np.zeros(4, np.float64)
         _check(lib().fwi_last_tile_timing(self._h, t.ctypes.data), "fwi_last_tile_timing")
+        return t
+
+    def last_recompute_timing(self):
+        """(ms, points) per interior tile launch of the checkpoint segment recompute, and the forward
+        steps the last call recomputed."""
+        t = np.zeros(3, np.float64)
+        _check(lib().fwi_last_recompute_timing(self._h, t.ctypes.data), "fwi_last_recompute_timing")
         return t

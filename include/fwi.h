@@ -267,6 +267,12 @@ int fwi_last_timing(void *ctx, float *out4);
  * the same for the adjoint; zeros when nothing was sampled. */
 int fwi_set_tile_timing(void *ctx, int on);
 int fwi_last_tile_timing(void *ctx, double *out4);
+/* With checkpoint storage the adjoint section also runs the forward steps of
+ * each segment's recompute (beside the adjoint steps, on their own streams):
+ * out[0] mean duration (ms) of their sampled interior tile launches, out[1]
+ * interior points such a launch updated, out[2] forward steps the last call
+ * recomputed (zeros without checkpoint storage or samples). */
+int fwi_last_recompute_timing(void *ctx, double *out3);
 
 /* How many of this library's kernels the last call launched. */
 long fwi_last_launches(void *ctx);

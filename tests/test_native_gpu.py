@@ -369,7 +369,7 @@ def test_graph_replay_matches_direct_issue_bitwise(exact_case, store, batch):
     ctx.set_model(*(np.ascontiguousarray(p[k], np.float32) for k in ("vh", "vp", "vn")))
     ctx.set_tile_timing(True)
     sh, ob = make_shots(shots), obs.astype(np.float32)
-    runs, launches, tiles = [], [], []
+    runs, launches, tiles, recs = [], [], [], []
     for i in range(4):  # direct, captured, replayed, replayed
         try:
             runs.append(ctx.gradient(sh, ob, mask))
@@ -377,6 +377,7 @@ def test_graph_replay_matches_direct_issue_bitwise(exact_case, store, batch):
             raise AssertionError(f"call {i}: {e}, cudaError {ctx.last_cuda_error()}") from e
         launches.append(ctx.last_launches())
         tiles.append(ctx.last_tile_timing())
+        recs.append(ctx.last_recompute_timing())
     replays = ctx.graph_replays()
     traces = [ctx.forward(sh) for _ in range(3)]
     assert ctx.graph_replays() > replays
@@ -389,6 +390,16 @@ def test_graph_replay_matches_direct_issue_bitwise(exact_case, store, batch):
     assert len(set(launches)) == 1 and direct_launches == launches[0]
     for t in tiles[1:]:
         assert np.all(t[[1, 3]] == tiles[0][[1, 3]]) and np.all(t[[0, 2]] > 0)
+    # the segment recompute's forward steps: counted and sampled alike in every call (the sampled
+    # launches' interior points may be zero: this small grid has no interior tile under the origin a
+    # batch of two windows takes)
+    for r in recs:
+        if store == "checkpoint":
+            assert r[2] == recs[0][2] > 0 and r[1] == recs[0][1] and r[0] >= 0
+        else:
+            assert np.all(r == 0)
+    if store == "checkpoint" and batch == 1:
+        assert recs[0][1] > 0 and all(r[0] > 0 for r in recs)
     for r in runs:
         assert r[0] == direct[0]
         for a, b in zip(r[1:], direct[1:]):
