@@ -1,7 +1,7 @@
 // Small shots resident on chip (FP32, exact adjoint, every step's images
 // kept): one thread-block cluster per shot, sm_103a.
 //
-// A shot whose grid fits the cluster's shared memory (C1: 209 x 209) gains
+// A shot whose grid fits the cluster's shared memory (e.g. 209 x 209) gains
 // nothing from the tile passes' per-step launches: one step of one small shot
 // is a few microseconds of work, less than the launch and dependency latency
 // of the two tile passes.  Here a cluster of up to 16 CTAs (a non-portable
@@ -52,7 +52,7 @@ namespace fwi {
 namespace cg = cooperative_groups;
 
 constexpr int kClusterMaxCtas = 16;
-constexpr int kClusterThreads = 704;  // 4 columns a thread: one pass over a CTA of C1's rows
+constexpr int kClusterThreads = 704;  // 4 columns a thread: one pass over 13 rows of a 209-wide window
 constexpr int kClHalo = 2 * kRad;  // halo rows of the copied fields
 
 // Interior rows of each CTA: CTA k owns interior rows [start[k], start[k + 1]) (global rows

@@ -85,6 +85,7 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
     __shared__ __align__(8) uint64_t bar[kLayerStages];
     __shared__ int act[kMaxGroup];
     __shared__ FwdShot ps[kMaxGroup];
+    __shared__ float wmax[2][kTmaThreads / 32];  // the warps' maxima of |P|, |F| of a shot (alternate shots)
     const int tid = threadIdx.x;
     int x0, z0;
     tile_origin(b, kTilesFwdLayer, x0, z0);
@@ -303,8 +304,16 @@ k_fwd_layer(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb
                 }
             }
         }
-        if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)act[a] * (b.nt_max + 1) + g + 1]);
+        if (Cd::scaled) {
+            for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+            if ((tid & 31) == 0) wmax[a & 1][tid >> 5] = lmax;
+        }
         __syncthreads();  // every thread is done with this stage
+        if (Cd::scaled && tid == 0) {  // one reduction per block and shot
+            float m = 0.f;
+            for (int w = 0; w < kTmaThreads / 32; w++) m = fmaxf(m, wmax[a & 1][w]);
+            if (m > 0.f) atomicMax((unsigned *)&b.amax[(long)act[a] * (b.nt_max + 1) + g + 1], __float_as_uint(m));
+        }
         if (tid == 0 && a + kLayerStages < na) {
             fence_proxy_async();
             issue(a + kLayerStages);

@@ -255,6 +255,7 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
     FwdShot *ps = reinterpret_cast<FwdShot *>(dsm + kStages * sizeof(FwdIncStage));
     int *act = reinterpret_cast<int *>(ps + sg);
     __shared__ __align__(8) uint64_t bar[kStages];
+    __shared__ float wmax[2][kTmaThreads / 32];  // the warps' maxima of |P|, |F| of a shot (alternate shots)
     const int tid = threadIdx.x;
     int x0, z0;
     tile_origin(b, kTilesFwdInterior, x0, z0);
@@ -414,8 +415,16 @@ k_fwd_tma(Batch<float> b, const __grid_constant__ TmaMaps maps, int g, int ntb, 
                 }
             }
         }
-        if (Cd::scaled) warp_max_to(lmax, &b.amax[(long)act[a] * (b.nt_max + 1) + g + 1]);
+        if (Cd::scaled) {
+            for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+            if ((tid & 31) == 0) wmax[a & 1][tid >> 5] = lmax;
+        }
         if (!stage_release(ok, bar, a, na, kStages, b.status)) return;  // every thread is done with this stage
+        if (Cd::scaled && tid == 0) {  // one reduction per block and shot
+            float m = 0.f;
+            for (int w = 0; w < kTmaThreads / 32; w++) m = fmaxf(m, wmax[a & 1][w]);
+            if (m > 0.f) atomicMax((unsigned *)&b.amax[(long)act[a] * (b.nt_max + 1) + g + 1], __float_as_uint(m));
+        }
         if (tid == 0 && a + kStages < na) {
             fence_proxy_async();
             issue(a + kStages);

@@ -109,3 +109,44 @@ def test_cluster_path_c1_grid_unequal_rows(c1_case, sprec, tol_tile, monkeypatch
     assert lc < 10 < lt
     assert abs(Jc - J) <= 1e-5 * J and abs(Jc - Jt) <= 1e-6 * Jt
     assert max(e_tile) <= tol_tile and max(e_or) <= (1e-4 if sprec == 0 else tol_tile)
+
+
+@pytest.mark.parametrize("shape", [
+    dict(nx=40, nz=44, cpml=4, nt=90),     # no CPML point inside the interior (layer width = frame)
+    dict(nx=96, nz=200, cpml=30, nt=80),   # 16 CTAs over 192 rows, wide layers (side band 52 of 88 columns)
+    dict(nx=72, nz=36, cpml=10, nt=3),     # 3 CTAs, three steps
+])
+def test_cluster_path_edge_shapes(shape, monkeypatch):
+    """Shapes at the edges of the cluster path's plan (no layer work, wide layers, a handful of
+    CTAs, a few steps), against the FP64 oracle and the tile passes, with random observed data;
+    source and receivers in the bottom layer, so that the two wavefields meet within the steps."""
+    p = exact_problem(seed=3, nx=shape["nx"], nz=shape["nz"], nt=shape["nt"])
+    p["cpml"] = shape["cpml"]
+    nx, nz, nt = p["nx"], p["nz"], p["nt"]
+    shots = [dict(sx=nx // 2, sz=nz - 6, rz=nz - 8, rx0=4, rx1=nx - 4, nt=nt, x0=0, nxw=0)]
+    rng = np.random.default_rng(2)
+    obs = 1e-3 * rng.standard_normal(nt * (nx - 8))
+    mask = np.ones(nx - 8, np.uint8)
+    J, g = oracle_exact(p, shots, obs, mask)
+    (Jc, *gc), lc, _ = run(p, shots, obs, mask)
+    (Jt, *gt), lt, _ = run(p, shots, obs, mask, cluster=False, monkeypatch=monkeypatch)
+    assert lc < 10 < lt
+    assert abs(Jc - J) <= 1e-5 * J and abs(Jc - Jt) <= 1e-6 * Jt
+    for a, b, c in zip(gc, g, gt):
+        assert np.linalg.norm(b) > 0
+        assert rel(a, b) <= 1e-4 and rel(a, c) <= 1e-5
+
+
+def test_cluster_path_single_step(monkeypatch):
+    """One step: the misfit of the first samples, a gradient of zeros (no image before the first
+    update), as the tile passes give."""
+    p = exact_problem(seed=3, nx=72, nz=36, nt=1)
+    nx, nz = p["nx"], p["nz"]
+    shots = [dict(sx=nx // 2, sz=nz - 6, rz=nz - 8, rx0=4, rx1=nx - 4, nt=1, x0=0, nxw=0)]
+    obs = 1e-3 * np.random.default_rng(4).standard_normal(nx - 8)
+    mask = np.ones(nx - 8, np.uint8)
+    (Jc, *gc), lc, _ = run(p, shots, obs, mask)
+    (Jt, *gt), _, _ = run(p, shots, obs, mask, cluster=False, monkeypatch=monkeypatch)
+    assert lc < 10 and abs(Jc - Jt) <= 1e-6 * Jt
+    for a, c in zip(gc, gt):
+        assert np.all(np.isfinite(a)) and np.allclose(a, c, rtol=1e-5, atol=1e-30)
