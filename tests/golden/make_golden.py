@@ -7,7 +7,7 @@ compiles src/parallelcalls.cu from the reference checkout for the CPU
 src/main.c does (launch grids of src/serialcalls.cu).  The inputs are small
 seeded synthetic models.
 
-Usage (needs the reference checkout; default /root/reference):
+Usage (needs the reference checkout, given by --ref-root or FWI_REFERENCE_ROOT):
     python tests/golden/make_golden.py [--ref-root PATH]
 
 Writes tests/golden/ref_small.npz.  Host-side inputs that src/main.c computes
