@@ -1079,6 +1079,18 @@ template <typename T> struct Ctx : CtxBase {
     };
     std::vector<Tuned> tuned;
 
+    // The order in which the shots of a call form batches: longest first (stable: shots of one
+    // length keep the caller's order).  A batch runs as many steps as its longest shot, its
+    // shorter shots idle until their own start, so batches of similar length keep the GPU busy;
+    // the gradient and misfit are sums over the shots.
+    static std::vector<int> batch_order(const std::vector<DevShot> &all)
+    {
+        std::vector<int> o(all.size());
+        for (size_t k = 0; k < o.size(); k++) o[k] = (int)k;
+        std::stable_sort(o.begin(), o.end(), [&](int a, int c) { return all[a].nt > all[c].nt; });
+        return o;
+    }
+
     // What the fastest choice depends on: shots in the batch, widest window,
     // one window for all, mode, image store type.
     std::vector<long> choice_key(const std::vector<DevShot> &bs, int nxm) const
@@ -1400,35 +1412,59 @@ template <typename T> struct Ctx : CtxBase {
         TRY(cudaMemsetAsync(misfit, 0, sizeof(double), st));
         TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
         float t_fwd = 0, t_adj = 0;
+        const std::vector<int> order = batch_order(all);
         for (int b0 = 0; b0 < n; b0 += B) {
             const int nb = std::min(B, n - b0);
             int ntb = 0, nxm = 0;
-            std::vector<DevShot> bs(all.begin() + b0, all.begin() + b0 + nb);
+            // the batch's shots (order[b0 ..]), their records and mask rows packed in that order;
+            // runs of consecutive shots of the caller's arrays move in one copy
+            std::vector<DevShot> bs(nb);
             std::vector<long> bmo(nb);
+            long nrec_elems = 0, nmask = 0;
             for (int k = 0; k < nb; k++) {
-                bs[k].rec_off = off[b0 + k] - off[b0];
-                bmo[k] = moff[b0 + k] - moff[b0];
+                bs[k] = all[order[b0 + k]];
+                bs[k].rec_off = nrec_elems;
+                bmo[k] = nmask;
+                nrec_elems += off[order[b0 + k] + 1] - off[order[b0 + k]];
+                nmask += moff[order[b0 + k] + 1] - moff[order[b0 + k]];
                 ntb = std::max(ntb, bs[k].nt);
                 nxm = std::max(nxm, bs[k].nx);
             }
-            const long nrec_elems = off[b0 + nb] - off[b0];
+            // copy(dst, src, per-shot offsets (records or mask rows), element size): runs of consecutive shots
+            auto gather = [&](void *dst, const void *src, const std::vector<long> &o, const std::vector<long> &dsto,
+                              size_t elem, cudaMemcpyKind kind) -> int {
+                for (int k = 0; k < nb;) {
+                    int e = k + 1;
+                    while (e < nb && order[b0 + e] == order[b0 + e - 1] + 1) e++;
+                    const int s0 = order[b0 + k];
+                    const long len = o[s0 + e - k] - o[s0];
+                    TRY(cudaMemcpyAsync((char *)dst + dsto[k] * elem, (const char *)src + o[s0] * elem, len * elem,
+                                        kind, st));
+                    k = e;
+                }
+                return FWI_OK;
+            };
+            std::vector<long> rec_dst(nb), mask_dst(nb);
+            for (int k = 0; k < nb; k++) {
+                rec_dst[k] = bs[k].rec_off;
+                mask_dst[k] = bmo[k];
+            }
             TRY(cudaMemcpyAsync(shots, bs.data(), nb * sizeof(DevShot), cudaMemcpyHostToDevice, st));
             TRY(cudaMemcpyAsync(mask_off, bmo.data(), nb * sizeof(long), cudaMemcpyHostToDevice, st));
-            if (obs_in)
-                TRY(cudaMemcpyAsync(obs, (const T *)obs_in + off[b0], nrec_elems * sizeof(T), cudaMemcpyDefault, st));
-            else if (from_store && ostore)
-                TRY(cudaMemcpyAsync(obs, ostore + off[b0], nrec_elems * sizeof(T), cudaMemcpyDeviceToDevice, st));
-            else if (from_store)
+            if (obs_in) {
+                if ((rc = gather(obs, obs_in, off, rec_dst, sizeof(T), cudaMemcpyDefault))) return rc;
+            } else if (from_store && ostore) {
+                if ((rc = gather(obs, ostore, off, rec_dst, sizeof(T), cudaMemcpyDeviceToDevice))) return rc;
+            } else if (from_store)
                 for (int k = 0; k < nb; k++) {
-                    const int nr = all[b0 + k].rx1 - all[b0 + k].rx0;
-                    k_trace_decode<T><<<eg((long)all[b0 + k].nt * nr), 256, 0, st>>>(
-                        ostore_h, off[b0 + k], all[b0 + k].nt, nr, ostore_scale + moff[b0 + k], obs,
-                        off[b0 + k] - off[b0]);
+                    const int s0 = order[b0 + k];
+                    const int nr = all[s0].rx1 - all[s0].rx0;
+                    k_trace_decode<T><<<eg((long)all[s0].nt * nr), 256, 0, st>>>(
+                        ostore_h, off[s0], all[s0].nt, nr, ostore_scale + moff[s0], obs, bs[k].rec_off);
                     TRY_LAUNCH();
                     launches++;
                 }
-            if (mask_in)
-                TRY(cudaMemcpyAsync(mask, mask_in + moff[b0], moff[b0 + nb] - moff[b0], cudaMemcpyDefault, st));
+            if (mask_in && (rc = gather(mask, mask_in, moff, mask_dst, 1, cudaMemcpyDefault))) return rc;
             const size_t lb = (size_t)nb * slot * sizeof(T);
             for (auto &p : lvl) TRY(cudaMemsetAsync(p, 0, lb, st));
             for (int k = 0; k < 4; k++) TRY(cudaMemsetAsync(cp[k], 0, lb, st));
@@ -1534,8 +1570,15 @@ template <typename T> struct Ctx : CtxBase {
                 TRY_LAUNCH();
                 launches += 2;
             }
-            if (traces)
-                TRY(cudaMemcpyAsync((T *)traces + off[b0], rec, nrec_elems * sizeof(T), cudaMemcpyDefault, st));
+            if (traces)  // back to the caller's order, runs of consecutive shots in one copy
+                for (int k = 0; k < nb;) {
+                    int e = k + 1;
+                    while (e < nb && order[b0 + e] == order[b0 + e - 1] + 1) e++;
+                    const int s0 = order[b0 + k];
+                    TRY(cudaMemcpyAsync((T *)traces + off[s0], rec + bs[k].rec_off,
+                                        (off[s0 + e - k] - off[s0]) * sizeof(T), cudaMemcpyDefault, st));
+                    k = e;
+                }
             if (want_grad && on_cluster) {
                 NvtxRange adj_range("fwi adjoint steps + imaging");
                 for (auto &p : gs) TRY(cudaMemsetAsync(p, 0, lb, st));
@@ -1872,12 +1915,16 @@ template <typename T> struct Ctx : CtxBase {
         if (rc) return rc;
         const bool exact = cfg.mode == FWI_MODE_EXACT;
         const bool tiles = sizeof(T) == 4 && use_tma;  // the choices only steer the FP32 tile passes
+        const std::vector<int> order = batch_order(all);  // the batches gradient calls form
         for (int b0 = 0; b0 < n; b0 += B) {
             const int nb = std::min(B, n - b0);
-            std::vector<DevShot> bs(all.begin() + b0, all.begin() + b0 + nb);
+            std::vector<DevShot> bs(nb);
             int ntb = 0, nxm = 0;
+            long ro = 0;
             for (int k = 0; k < nb; k++) {
-                bs[k].rec_off = off[b0 + k] - off[b0];
+                bs[k] = all[order[b0 + k]];
+                bs[k].rec_off = ro;
+                ro += off[order[b0 + k] + 1] - off[order[b0 + k]];
                 ntb = std::max(ntb, bs[k].nt);
                 nxm = std::max(nxm, bs[k].nx);
             }
@@ -2085,9 +2132,11 @@ template <typename T> struct Ctx : CtxBase {
             if (rc) return rc;
         }
         std::vector<std::pair<std::vector<long>, Choices>> add;
+        const std::vector<int> order = batch_order(all);  // the batches gradient calls form
         for (int b0 = 0; b0 < n; b0 += B) {
             const int nb = std::min(B, n - b0);
-            std::vector<DevShot> bs(all.begin() + b0, all.begin() + b0 + nb);
+            std::vector<DevShot> bs(nb);
+            for (int k = 0; k < nb; k++) bs[k] = all[order[b0 + k]];
             int nxm = 0;
             for (const DevShot &d : bs) nxm = std::max(nxm, d.nx);
             Choices cb = c;

@@ -490,3 +490,39 @@ def test_a_wait_that_gives_up_is_reported_and_the_context_stays_usable(exact_cas
     assert again[0] == first[0]
     for a, b in zip(again[1:], first[1:]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("cluster", ["1", "0"])
+def test_shots_of_uneven_length_batch_by_length_in_any_caller_order(cluster, monkeypatch):
+    """A call forms its batches longest shot first (a batch runs as many steps as its longest
+    shot): the traces come back in the caller's order, bit for bit whatever that order, and the
+    misfit and gradients of a permuted call agree to FP32 rounding (the sums run in another order)."""
+    from fwi_gb300 import Context, MODE_EXACT, PREC_FP32, make_shots
+    monkeypatch.setenv("FWI_CLUSTER", cluster)  # the cluster path (this window fits) and the tile passes
+    p = exact_problem(seed=17, nx=72, nz=56, nt=260)
+    nx = p["nx"]
+    shots = [dict(sx=20 + 8 * k, sz=6, rz=5, rx0=4, rx1=nx - 4, nt=nt, x0=0, nxw=0)
+             for k, nt in enumerate((150, 260, 200, 260, 90))]
+    rng = np.random.default_rng(8)
+    obs = [1e-3 * rng.standard_normal(s["nt"] * (nx - 8)) for s in shots]
+    masks = [(rng.random(nx - 8) > 0.1).astype(np.uint8) for _ in shots]
+
+    def call(idx):
+        ctx = Context(nx=nx, nz=p["nz"], dh=p["dh"], dt=p["dt"], cpml=p["cpml"], f_cpml=p["f"], nt_max=p["nt"],
+                      max_shots=2, mode=MODE_EXACT, precision=PREC_FP32)
+        ctx.set_wavelet(wavelet(p).astype(np.float32))
+        ctx.set_model(*(np.ascontiguousarray(p[k], np.float32) for k in ("vh", "vp", "vn")))
+        sh = make_shots([shots[k] for k in idx])
+        r = ctx.gradient(sh, np.concatenate([obs[k] for k in idx]).astype(np.float32),
+                         np.concatenate([masks[k] for k in idx]))
+        tr = ctx.forward(sh)
+        cuts = np.cumsum([0] + [shots[k]["nt"] * (nx - 8) for k in idx])
+        return r, {k: tr[cuts[i]:cuts[i + 1]] for i, k in enumerate(idx)}
+
+    (J0, *g0), t0 = call([0, 1, 2, 3, 4])
+    (J1, *g1), t1 = call([4, 2, 0, 3, 1])
+    for k in t0:
+        assert np.array_equal(t0[k], t1[k])
+    assert abs(J1 - J0) <= 1e-6 * J0
+    for a, b in zip(g0, g1):
+        assert rel_l2(a, b) <= 1e-6, rel_l2(a, b)
