@@ -238,7 +238,10 @@ __device__ __forceinline__ void cl_cp_async16(void *dst, const void *src)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cl_cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cl_cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+template <int N> __device__ __forceinline__ void cl_cp_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 // Max over the CTA of v >= 0, pushed by thread 0 into slot k of every CTA's table (no remote
 // read after the barrier: each CTA reduces its own copy).

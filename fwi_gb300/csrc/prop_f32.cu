@@ -291,9 +291,12 @@ bool cluster_shot_fits(int nx_max, int nz, int cpml, int store_type)
     if (!cached_cluster_plan(nx_max, nz, cpml, store_type, p)) return false;
     // every kernel may take the device's whole opt-in shared memory: one setting serves all widths
     const size_t lim = cluster_smem_limit();
-    for (cudaError_t e : {cluster_attrs(k_cluster_fwd<kStoreNative>, lim), cluster_attrs(k_cluster_fwd<kStoreHalf>, lim),
-                          cluster_attrs(k_cluster_fwd<kStoreBf16>, lim), cluster_attrs(k_cluster_adj<kStoreNative>, lim),
-                          cluster_attrs(k_cluster_adj<kStoreHalf>, lim), cluster_attrs(k_cluster_adj<kStoreBf16>, lim)})
+    for (cudaError_t e : {cluster_attrs(k_cluster_fwd<kStoreNative>, lim),
+                          cluster_attrs(k_cluster_fwd<kStoreHalf>, lim),
+                          cluster_attrs(k_cluster_fwd<kStoreBf16>, lim),
+                          cluster_attrs(k_cluster_adj<kStoreNative>, lim),
+                          cluster_attrs(k_cluster_adj<kStoreHalf>, lim),
+                          cluster_attrs(k_cluster_adj<kStoreBf16>, lim)})
         if (e != cudaSuccess) {
             cudaGetLastError();
             return false;
@@ -324,10 +327,11 @@ cudaError_t launch_cluster_forward(const Batch<float> &b, int nx_max, int ntb, b
     if (!cached_cluster_plan(nx_max, b.nz, b.cpml, b.store_type, p)) return cudaErrorInvalidValue;
     const int img = images ? 1 : 0, n = p.ncta;
     const size_t sm = p.smem_fwd;
+    const int h = p.h, pt = p.pitch;
     switch (b.store_type) {
-    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, img);
-    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, img);
-    default: return cluster_launch(k_cluster_fwd<kStoreNative>, n, b.B, sm, st, b, p.rows, ntb, p.h, p.pitch, img);
+    case kStoreHalf: return cluster_launch(k_cluster_fwd<kStoreHalf>, n, b.B, sm, st, b, p.rows, ntb, h, pt, img);
+    case kStoreBf16: return cluster_launch(k_cluster_fwd<kStoreBf16>, n, b.B, sm, st, b, p.rows, ntb, h, pt, img);
+    default: return cluster_launch(k_cluster_fwd<kStoreNative>, n, b.B, sm, st, b, p.rows, ntb, h, pt, img);
     }
 }
 
