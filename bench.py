@@ -496,6 +496,36 @@ def single_shot_c1(args, fwi_gb300, torch, dev, steps=10, warmup=3):
         del c
     os.environ.pop("FWI_CLUSTER", None)
     out["cluster_speedup_over_tile_passes"] = round(out["cluster"]["value"] / out["tile_passes"]["value"], 3)
+    # the same small shots in a batch: one cluster per shot, the clusters side by side on the GPU
+    nb = 8
+    base = w.shots[0]
+    many = [dict(base, sx=int(8 + (w.nx - 16) * (k + 0.5) / nb)) for k in range(nb)]
+    sh8 = fwi_gb300.make_shots(many)
+    for name, flag in (("cluster_batch_of_8", "1"), ("tile_passes_batch_of_8", "0")):
+        os.environ["FWI_CLUSTER"] = flag
+        c = fwi_gb300.Context(nx=w.nx, nz=w.nz, dh=w.dh, dt=w.dt, cpml=w.cpml, f_cpml=w.f, nt_max=w.nt,
+                              max_shots=nb, max_receivers=w.nx, mode=fwi_gb300.MODE_EXACT,
+                              precision=fwi_gb300.PREC_FP32, store_prec=sprec, store=fwi_gb300.STORE_FULL,
+                              device=dev)
+        c.set_ricker(w.f, w.nt)
+        c.set_model(*w.squared())
+        obs8 = torch.zeros(nb * w.nt * (base["rx1"] - base["rx0"]), dtype=torch.float32, device="cuda")
+        c.forward(sh8, out=obs8)
+        c.set_model(*w.squared(initial=True))
+        g = [torch.zeros((w.nz, w.nx), dtype=torch.float32, device="cuda") for _ in range(3)]
+        for _ in range(warmup):
+            c.gradient(sh8, obs8, out=g)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            c.gradient(sh8, obs8, out=g)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"value": round(nb * 1e3 / ms, 3), "unit": "shots/s", "shots": nb, "ms_per_gradient": round(ms, 3)}
+        del c
+    os.environ.pop("FWI_CLUSTER", None)
     return out
 
 
