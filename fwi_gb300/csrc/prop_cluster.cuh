@@ -301,6 +301,7 @@ k_cluster_fwd(Batch<float> b, const __grid_constant__ ClRows rows, int ntb, int 
     using SI = typename Cd::S;
     extern __shared__ __align__(16) float csm[];
     __shared__ float s_all[2][kClusterMaxCtas];
+    __shared__ float s_sc;  // the next step's image scale, from every CTA's max (thread 0 computes it)
     cg::cluster_group cl = cg::this_cluster();
     const int ncta = (int)cl.num_blocks();
     const int s = blockIdx.x / ncta;
@@ -340,7 +341,7 @@ k_cluster_fwd(Batch<float> b, const __grid_constant__ ClRows rows, int ntb, int 
     const int nbx = cpml > 4 ? min(2 * (cpml - 4), G.nxi) : 0;  // side-band columns of a row
     const int nq = (G.nxi + 3) / 4;                               // groups of 4 columns of a row
     SI *const imgb = img ? (SI *)b.store + (long)s * b.n_img * 2 * b.slot : nullptr;
-    float amax = 0.f;  // max |P|, |F| after the previous step, over the shot
+    if (threadIdx.x == 0) s_sc = Cd::scaled ? image_scale(0.f, b.inv_dh2) : 1.f;  // read after the psi barrier
     float wv_next = sh.nt > 0 ? b.wavelet[0] : 0.f;
     int cur = 0;
     for (int it = 0; it < sh.nt; it++) {
@@ -382,7 +383,7 @@ k_cluster_fwd(Batch<float> b, const __grid_constant__ ClRows rows, int ntb, int 
             cl_st4(PSZ + ib, ps);
         }
         __syncthreads();
-        const float sc = Cd::scaled ? image_scale(amax, inv_dh2) : 1.f;
+        const float sc = Cd::scaled ? s_sc : 1.f;
         if (img && Cd::scaled && G.k == 0 && threadIdx.x == 0) b.scale[(long)s * b.nt_max + g] = sc;
         float lmax = 0.f;
         bool sat = false;
@@ -486,11 +487,11 @@ k_cluster_fwd(Batch<float> b, const __grid_constant__ ClRows rows, int ntb, int 
         if (sat) atomicOr(b.status, kStatusSaturated);
         if (Cd::scaled) cl_push_max(cl, G, lmax, s_all[it & 1]);
         cl.sync();  // the new level, and every CTA's max, complete
-        if (Cd::scaled) {
+        if (Cd::scaled && threadIdx.x == 0) {  // read by every thread after the next step's psi barrier
             float m = 0.f;
             for (int r = 0; r < G.ncta; r++) m = fmaxf(m, s_all[it & 1][r]);
-            amax = m;
-            if (G.k == 0 && threadIdx.x == 0) b.amax[(long)s * (b.nt_max + 1) + g + 1] = m;
+            s_sc = image_scale(m, inv_dh2);
+            if (G.k == 0) b.amax[(long)s * (b.nt_max + 1) + g + 1] = m;
         }
         cur ^= 1;
     }
