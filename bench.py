@@ -340,7 +340,7 @@ def native_arm(args, rank, world, dist):
                          "adjoint_phase_frac_with_recompute": round((adj_bytes * pts + rec_bytes)
                                                                     / (t_adj / args.steps / 1e3) / 1e9 / hbm, 4),
                          "forward_step_frac": round(ALG_BYTES_FWD * pts / (t_fwd / args.steps / 1e3) / 1e9 / hbm, 4),
-                         # the survey's point-update basis: useful updates x 52 B (36 + 68, two updates)
+                         # the point-update basis: useful updates x 52 B (36 forward + 68 adjoint, two updates)
                          "gradient_frac": round(world * upd / (ms / 1e3) * (ALG_BYTES_FWD + ALG_BYTES_ADJ) / 2
                                                 / 1e9 / hbm, 4)},
             "gpu_launches": int(launches),
