@@ -16,6 +16,7 @@ scaling, no collective on the data path); rank 0 prints the aggregate.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -189,6 +190,7 @@ def config_of(args, w):
     return {"workload": w.name, "nx": w.nx, "nz": w.nz, "dh": w.dh, "dt": w.dt, "nt": w.nt,
             "shots": len(w.shots), "receivers_per_shot": nrec, "ricker_hz": w.f, "cpml": w.cpml,
             "mode": args.mode, "image_store": f"{args.storage}, {args.store}", "batch": args.batch,
+            **({"ckpt_every": args.ckpt_every} if args.ckpt_every > 0 else {}),
             "l2": f"inputs larger than L2 (observed data {ntr * 4 / 1e6:.0f} MB; the per-step state of "
                   f"all shots {6 * 4 * w.nz * w.nx * len(w.shots) / 1e6:.0f} MB; images or rings streamed "
                   f"through HBM)"}
@@ -215,7 +217,8 @@ def native_arm(args, rank, world, dist):
     def context(max_shots, precision=fwi_gb300.PREC_FP32, store_prec=sprec, store=args.storage):
         c = fwi_gb300.Context(nx=w.nx, nz=w.nz, dh=w.dh, dt=w.dt, cpml=w.cpml, f_cpml=w.f, nt_max=w.nt,
                               max_shots=max_shots, max_receivers=nrec, max_window=max_window, mode=mode,
-                              precision=precision, store_prec=store_prec, store=store_of[store], device=dev)
+                              precision=precision, store_prec=store_prec, store=store_of[store],
+                              ckpt_every=args.ckpt_every, device=dev)
         c.set_ricker(w.f, w.nt)
         return c
 
@@ -307,6 +310,8 @@ def native_arm(args, rank, world, dist):
         rec_bytes = (ALG_BYTES_FWD + img_write) * rec_pts * rec_steps
         r = {
             "value": round(world * nshots / (ms / 1e3), 4), "ms_per_step": round(ms, 3), "misfit": J,
+            # device memory of the context by fwi_config_bytes (the storage mode's figure)
+            "device_gb": round(fwi_gb300.native.lib().fwi_config_bytes(ctypes.byref(ctx.cfg)) / 1e9, 2),
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
                     "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
@@ -373,7 +378,7 @@ def native_arm(args, rank, world, dist):
             "gpt_updates_counted_on": f"updated points: {w.nx - 8} x {w.nz - 8} per shot and step, forward and "
                                       f"adjoint (the 4-point frame excluded)",
             "e2e": head["e2e"], "roofline": head["roofline"], "gpu_launches": head["gpu_launches"],
-            "phase_ms": head["phase_ms"], "misfit": head["misfit"],
+            "phase_ms": head["phase_ms"], "misfit": head["misfit"], "device_gb": head["device_gb"],
         }
         if "clocks" in head:
             out["clocks"] = head["clocks"]
@@ -677,6 +682,8 @@ def main():
     ap.add_argument("--store", default="fp16", choices=["fp32", "fp16", "bf16"])
     ap.add_argument("--storage", default="checkpoint", choices=["full", "checkpoint", "boundary"],
                     help="how the forward images are kept (FWI_STORE_*) in the headline run")
+    ap.add_argument("--ckpt-every", type=int, default=0,
+                    help="checkpoint interval in steps (0: automatic, the one that needs the least memory)")
     ap.add_argument("--plain-shots", type=int, default=4)
     ap.add_argument("--accuracy-shots", type=int, default=8, help="shots of the FP64 comparison")
     ap.add_argument("--invert-iters", type=int, default=20,
