@@ -239,6 +239,8 @@ def native_arm(args, rank, world, dist):
         """Gradient shots/s of the whole batch with `storage`: device-resident `value`, then e2e through
         fwi_gradient with pinned host buffers."""
         ctx = context(min(args.batch, len(w.shots)), store=storage)
+        # device memory of the context by fwi_config_bytes (the storage mode's figure)
+        device_gb = round(fwi_gb300.native.lib().fwi_config_bytes(ctypes.byref(ctx.cfg)) / 1e9, 2)
         ctx.set_model(*w.squared(initial=True))
         g_d = [torch.zeros((w.nz, w.nx), dtype=torch.float32, device="cuda") for _ in range(3)]
         # launch choice: measured by the autotuner (before the warm-up, untimed) or the built-in one
@@ -310,8 +312,7 @@ def native_arm(args, rank, world, dist):
         rec_bytes = (ALG_BYTES_FWD + img_write) * rec_pts * rec_steps
         r = {
             "value": round(world * nshots / (ms / 1e3), 4), "ms_per_step": round(ms, 3), "misfit": J,
-            # device memory of the context by fwi_config_bytes (the storage mode's figure)
-            "device_gb": round(fwi_gb300.native.lib().fwi_config_bytes(ctypes.byref(ctx.cfg)) / 1e9, 2),
+            "device_gb": device_gb,
             "gpt_updates_per_s": round(world * upd / (ms / 1e3) / 1e9, 3),
             "e2e": {"value": round(world * nshots / (ms_e2e / 1e3), 4), "unit": "shots/s",
                     "h2d_bytes_per_step": int(ntr * 4), "d2h_bytes_per_step": int(3 * w.nx * w.nz * 4 + 8)},
