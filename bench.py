@@ -390,7 +390,8 @@ def native_arm(args, rank, world, dist):
             o = measure(other, False)
             if rank == 0:
                 out.setdefault("other_storage", {})[other] = {
-                    k: o[k] for k in ("value", "ms_per_step", "gpt_updates_per_s", "phase_ms", "launch_choice")
+                    k: o[k] for k in ("value", "ms_per_step", "gpt_updates_per_s", "phase_ms", "launch_choice",
+                                      "device_gb")
                 } | {"e2e": o["e2e"]["value"], "roofline_frac": o["roofline"]["frac"],
                      "gradient_frac": o["roofline"]["gradient_frac"]}
 
