@@ -94,3 +94,23 @@ def test_invalid_configuration_is_rejected_before_any_device_call(built):
 def test_strerror_covers_every_status(built):
     for s in range(0, -8, -1):
         assert built.fwi_strerror(s).decode() != "unknown status"
+
+
+def test_checkpoint_interval_trades_memory_for_recompute(built):
+    """The automatic interval (0) is the memory-minimal one (checkpoints + the two-segment image
+    buffer, within the rounding of the segment count); a longer one costs memory in proportion.
+    C2 batch: 609 x 309 grid, nt 3000, 32 shots, FP16 images."""
+    def gb(k):
+        cfg = native.Config()
+        built.fwi_config_default(C.byref(cfg))
+        cfg.nx, cfg.nz, cfg.dh, cfg.dt, cfg.cpml, cfg.f_cpml = 609, 309, 10.0, 0.001, 20, 8.0
+        cfg.nt_max, cfg.max_shots, cfg.max_window, cfg.max_receivers = 3000, 32, 609, 601
+        cfg.mode, cfg.store, cfg.store_prec = native.MODE_EXACT, native.STORE_CHECKPOINT, native.SPREC_FP16
+        cfg.ckpt_every = k
+        return built.fwi_config_bytes(C.byref(cfg)) / 1e9
+
+    auto = gb(0)
+    assert auto == gb(110)  # ceil(sqrt(8 nt / (4 * 0.5)))
+    assert auto <= 1.01 * min(gb(k) for k in range(20, 400))
+    assert auto < gb(375) < gb(750) < gb(3000)
+    assert round(auto, 1) == 12.4 and round(gb(375), 1) == 21.8 and round(gb(750), 1) == 39.9
