@@ -2399,7 +2399,8 @@ int fwi_create(const fwi_config *cfg, void **out)
     if (!cfg || !out) return FWI_ERR_ARG;
     *out = nullptr;
     if (cfg->nx < 2 * cfg->cpml + 9 || cfg->nz < cfg->cpml + 9 || cfg->cpml < 0 || cfg->nt_max <= 0 ||
-        cfg->max_shots <= 0 || !(cfg->dh > 0) || !(cfg->dt > 0) || cfg->max_window < 0 || cfg->max_window > cfg->nx)
+        cfg->max_shots <= 0 || !(cfg->dh > 0) || !(cfg->dt > 0) || cfg->max_window < 0 || cfg->max_window > cfg->nx ||
+        cfg->ckpt_every < 0 || cfg->device < 0)
         return FWI_ERR_ARG;
     if (cfg->mode != FWI_MODE_EXACT && cfg->mode != FWI_MODE_REF_COMPAT) return FWI_ERR_ARG;
     if (cfg->store != FWI_STORE_FULL && cfg->store != FWI_STORE_CHECKPOINT && cfg->store != FWI_STORE_BOUNDARY)

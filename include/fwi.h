@@ -75,8 +75,9 @@ typedef struct {
     int precision;    /* FWI_PREC_* */
     int store;        /* FWI_STORE_* */
     int store_prec;   /* FWI_SPREC_* */
-    int ckpt_every;   /* checkpoint interval for FWI_STORE_CHECKPOINT (0 = automatic) */
-    int device;       /* CUDA device ordinal */
+    int ckpt_every;   /* checkpoint interval for FWI_STORE_CHECKPOINT (0 = automatic: the least
+                         memory; a longer one recomputes fewer steps); >= 0 */
+    int device;       /* CUDA device ordinal, >= 0 */
 } fwi_config;
 
 /* One shot.  Coordinates are 0-based model grid points.  The simulation grid

@@ -85,7 +85,7 @@ def test_config_defaults_and_bytes(built):
 
 def test_invalid_configuration_is_rejected_before_any_device_call(built):
     for bad in (dict(nx=20), dict(cpml=-1), dict(nt_max=0), dict(max_shots=0), dict(mode=7),
-                dict(max_window=10_000)):
+                dict(max_window=10_000), dict(ckpt_every=-1), dict(device=-1)):
         with pytest.raises(native.FwiError) as e:
             native.Context(**bad)
         assert e.value.status == native.FWI_ERR_ARG
