@@ -6,6 +6,9 @@
 //   main stream:  interior tiles (prop_tma.cuh)
 // joined before the next step.  Both tile passes read only the current time
 // level and write disjoint points.  The generic passes of prop.cuh serve FP64.
+// Small shots with full storage take the other route: one thread-block cluster
+// per shot runs every step of a phase in one launch (prop_cluster.cuh;
+// launch_cluster_forward / launch_cluster_adjoint below).
 #include <mutex>
 
 #include "prop_boundary.cuh"
